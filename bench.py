@@ -1,0 +1,359 @@
+"""Benchmark of the FFT -> |X| -> peaks path on one GB300 (JSON line on stdout).
+
+Workload ("plain large"): 256 beams x 65536 complex64 samples, Hann window,
+zero-padded to nFFT = 131072, all strict local maxima of |X| above the
+6-sigma noise threshold, compacted, parabolic sub-bin refinement.
+A step = one call of spx_fft_peaks over the whole batch with the input
+already in device memory.  Three input buffers rotate so every step reads
+384 MiB-apart data (inputs larger than L2 between steps).
+
+value = Msamples/s = beams * n_point / step time (input samples, before
+padding), max over ranks; e2e = the same through the C ABI from pinned host
+memory with the host->device copy of the samples and the device->host copy
+of the maxima and counts inside the timed region.
+
+--impl reference times the reference's CPU path on the host cores instead:
+pocketfft FP32 (scipy.fft, the library the reference vendors for its CPU FFT)
++ the CPU restatement of |X| and the peak search, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BEAMS, N_POINT, NFFT = 256, 65536, 131072
+FS = 1.0
+SIGMA = 6.0
+METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
+WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
+
+
+def _parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample-beams", type=int, default=0)
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+# ---------------------------------------------------------------------------
+# CPU path (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+def cpu_path_sample(x: np.ndarray, workers: int):
+    """pocketfft FP32 FFT over the beams (scipy.fft, `workers` threads) + |X| +
+    thresholded all-maxima search; returns the number of maxima found."""
+    import scipy.fft as sf
+
+    from oracle import spectrum_oracle as orc
+    xw = orc.windowed(x, orc.WINDOW_HANN)
+    spec = sf.fft(xw, n=NFFT, axis=-1, workers=workers)
+    assert spec.dtype == np.complex64
+    mag = orc.mag_rn(spec)
+    start, end, cap = orc.all_maxima_capacity(NFFT, 0, 0, 1000)
+    thr = orc.noise_threshold(mag, start, end, orc.noise_threshold_factor(SIGMA))
+    total = 0
+    for b in range(x.shape[0]):
+        total += len(orc.local_maxima(mag[b], start, end, thr[b]))
+    return total
+
+
+def cpu_measure(sample_beams: int, reps_budget_s: float = 15.0):
+    from spectrum_gb300 import synth
+    bs = synth.workload_large(seed=1, beams=sample_beams)
+    x = synth.synth_numpy(bs)
+    cores = os.cpu_count() or 1
+    cpu_path_sample(x, cores)  # warm caches / plans
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        cpu_path_sample(x, cores)
+        reps += 1
+        if time.perf_counter() - t0 > reps_budget_s or reps >= 50:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    msps = sample_beams * N_POINT / dt / 1e6
+    return msps, cores, f"{sample_beams} beams x {N_POINT} of the same workload, {reps} repetitions"
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    beams = args.cpu_sample_beams or 16
+    # each step is one bounded sample; warmup + steps sized to stay within minutes
+    from spectrum_gb300 import synth
+    bs = synth.workload_large(seed=1, beams=beams)
+    x = synth.synth_numpy(bs)
+    cores = os.cpu_count() or 1
+    for _ in range(max(args.warmup, 1)):
+        cpu_path_sample(x, cores)
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_path_sample(x, cores)
+        t.append(time.perf_counter() - t0)
+    step = sum(t) / len(t)
+    value = beams * N_POINT / step / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_beams": beams, "cpu_threads": cores},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Msamples/s", "cores": cores, "kind": "port",
+                         "sample": f"{beams} beams x {N_POINT} per step (pocketfft FP32 via scipy.fft + "
+                                   f"CPU restatement of |X| and the thresholded all-maxima search)"},
+        "e2e": {"value": round(value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.rows = []
+        self.proc = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for i, n in enumerate(names):
+                    if r[5 + i].lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import spectrum_gb300 as spx
+    from spectrum_gb300 import synth
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream(dev)
+    ctx = spx.default_context(local)
+
+    # three rotating input buffers (different seeds) -> inputs larger than L2
+    nbuf = 3
+    xs = [synth.synth_torch(synth.workload_large(seed=1 + 97 * rank + i, beams=BEAMS), device=dev)
+          for i in range(nbuf)]
+    torch.cuda.synchronize()
+    _, _, cap = spx._capi.all_maxima_capacity(NFFT, 0, 0, 1000)
+    out = torch.empty((BEAMS, cap, 8), dtype=torch.int32, device=dev)
+    counts = torch.empty(BEAMS, dtype=torch.int32, device=dev)
+    import ctypes as C
+    p = spx.peak_params(spx.PEAK_ALL, 0, 0, 0, 1000, spx.REFINE_PARABOLIC, FS, SIGMA)
+
+    def step(i):
+        ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(xs[i % nbuf].data_ptr()), BEAMS, N_POINT, NFFT,
+                                        spx.WINDOW_HANN, C.byref(p), C.c_void_p(out.data_ptr()),
+                                        C.c_void_p(counts.data_ptr())))
+
+    ctx.bind_stream(stream)
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * BEAMS * N_POINT / (ms * 1e-3) / 1e6
+
+    # ---- per-kernel timing of the dominant kernel (CUDA events, same stream) ----
+    kern = time_components(spx, ctx, xs, out, counts, p, stream, args.steps)
+
+    # ---- end to end from pinned host memory ----
+    e2e = time_e2e(spx, ctx, xs[0], out, counts, p, stream, args)
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (the FFT, which reads the samples once)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Msamples/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
+        "data": "synthetic (seeded tones + noise, SNR U[0,40] dB)",
+        "config": {"workload": WORKLOAD, "beams": BEAMS, "n_point": N_POINT, "nfft": NFFT,
+                   "window": "hann", "thresh_sigma": SIGMA, "refine": "parabolic",
+                   "l2": "3 rotating 128 MiB input buffers (inputs larger than L2)",
+                   "path": kern["path"]},
+        "roofline": kern["roofline"] | {"peak": hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "components_ms": kern["components_ms"],
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": kern["launches_per_step"] * args.steps,
+    }
+    r = line["roofline"]
+    r["frac"] = round(r["achieved"] / r["peak"], 4)
+    if args.cpu_sample_beams >= 0:
+        v, cores, sample = cpu_measure(args.cpu_sample_beams or 8)
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "Msamples/s", "cores": cores, "kind": "port",
+                                "sample": sample}
+    print(json.dumps(line), flush=True)
+
+
+def time_components(spx, ctx, xs, out, counts, p, stream, steps):
+    """Times the launches of one step separately with CUDA events on the stream."""
+    import ctypes as C
+
+    import torch
+    spec = torch.empty((BEAMS, NFFT), dtype=torch.complex64, device=xs[0].device)
+    n = max(steps, 5)
+    fft_ms, peak_ms = [], []
+    for i in range(n):
+        x = xs[i % len(xs)]
+        e0, e1, e2 = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e0.record(stream)
+        ctx.check(spx.lib.spx_fft(ctx.h, C.c_void_p(x.data_ptr()), BEAMS, N_POINT, NFFT, spx.WINDOW_HANN,
+                                  spx.OUT_COMPLEX, 1.0, C.c_void_p(spec.data_ptr())))
+        e1.record(stream)
+        ctx.check(spx.lib.spx_all_maxima(ctx.h, None, C.c_void_p(spec.data_ptr()), BEAMS, NFFT, C.byref(p),
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(counts.data_ptr())))
+        e2.record(stream)
+        torch.cuda.synchronize()
+        fft_ms.append(e0.elapsed_time(e1))
+        peak_ms.append(e1.elapsed_time(e2))
+    f = statistics.median(fft_ms)
+    algo = BEAMS * N_POINT * 8 + BEAMS * NFFT * 8  # read samples + write spectrum
+    return {
+        "path": "composed: fft_out_kernel (COMPLEX) + noise_hist/select + all_maxima_kernel",
+        "components_ms": {"fft": round(f, 4), "peaks": round(statistics.median(peak_ms), 4)},
+        "roofline": {"bound": "hbm", "kernel": "fft_out_kernel", "achieved": round(algo / (f * 1e-3) / 1e9, 1),
+                     "unit": "GB/s", "traffic": None,
+                     "algorithmic_bytes_per_launch": algo},
+        "launches_per_step": 4,
+    }
+
+
+def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
+    import ctypes as C
+
+    import torch
+    host_in = torch.empty(x_dev.shape, dtype=x_dev.dtype, pin_memory=True)
+    host_in.copy_(x_dev.cpu())
+    host_out = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+    host_cnt = torch.empty(counts.shape, dtype=counts.dtype, pin_memory=True)
+    dev_in = torch.empty_like(x_dev)
+
+    def step():
+        dev_in.copy_(host_in, non_blocking=True)
+        ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(dev_in.data_ptr()), BEAMS, N_POINT, NFFT,
+                                        spx.WINDOW_HANN, C.byref(p), C.c_void_p(out.data_ptr()),
+                                        C.c_void_p(counts.data_ptr())))
+        host_out.copy_(out, non_blocking=True)
+        host_cnt.copy_(counts, non_blocking=True)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(args.steps // 2, 3)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": round(BEAMS * N_POINT / (ms * 1e-3) / 1e6, 2), "unit": "Msamples/s",
+            "ms_per_step": round(ms, 4), "h2d_bytes_per_step": int(host_in.numel() * 8),
+            "d2h_bytes_per_step": int(host_out.numel() * 4 + host_cnt.numel() * 4)}
+
+
+def main():
+    args = _parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

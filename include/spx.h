@@ -1,0 +1,221 @@
+/*
+ * spx.h — C ABI of the GB300 FFT-to-peaks path (spectrum_gb300).
+ *
+ * This is the drop-in boundary for DspSpectrum's FFT -> |X| -> peaks hot path.
+ * Every entry point takes plain pointers and sizes, returns an spx_status and
+ * never throws.  Device pointers are borrowed; nothing returned here is owned
+ * by the caller unless the comment says so.  All work is ordered on the
+ * context's CUDA stream (spx_set_stream); entry points that fill device
+ * buffers return before the GPU finishes, exactly like the reference's
+ * *ToGPU / *ToBuffer calls.
+ *
+ * Mapping to the reference (paths relative to the DspSpectrum project):
+ *   spx_fft                -> FFTProcessorROCm::ProcessComplex / ProcessMagPhase /
+ *                             ProcessMagnitudesToGPU
+ *                             (include/spectrum/fft_processor_rocm.hpp:74-124;
+ *                              src/fft_func/src/fft_processor_rocm.cpp:306-659)
+ *   spx_magnitude          -> ComplexToMagPhaseROCm::ProcessMagnitudeToBuffer /
+ *                             ProcessMagnitudeToGPU / ProcessMagnitude
+ *                             (include/spectrum/complex_to_mag_phase_rocm.hpp:187-225;
+ *                              src/fft_func/src/complex_to_mag_phase_rocm.cpp:322-410)
+ *   spx_mag_phase          -> ComplexToMagPhaseROCm::Process / ProcessToGPU
+ *                             (complex_to_mag_phase_rocm.hpp:115-168)
+ *   spx_peaks_one_two      -> SpectrumProcessorROCm post kernels (ONE_PEAK / TWO_PEAKS)
+ *                             (include/spectrum/kernels/fft_kernel_sources_rocm.hpp:122-519,
+ *                              src/fft_func/src/spectrum_processor_rocm.cpp:1030-1122)
+ *   spx_all_maxima         -> IAllMaximaPipeline::Execute
+ *                             (include/spectrum/interface/i_all_maxima_pipeline.hpp:71-80,
+ *                              src/fft_func/src/all_maxima_pipeline_rocm.cpp:258-472)
+ *   spx_topk               -> (no reference counterpart: top-K of local maxima)
+ *   spx_fft_peaks          -> ISpectrumProcessor::ProcessFromGPU / FindAllMaximaFromGPUPipeline
+ *                             fused into one launch (include/spectrum/interface/
+ *                             i_spectrum_processor.hpp:95-129)
+ */
+#ifndef SPX_H_
+#define SPX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPX_ABI_VERSION 1
+
+/* Status codes.  The C++ facades map INVALID_ARG to std::invalid_argument and
+ * every other non-zero code to std::runtime_error, as the reference throws
+ * (e.g. src/fft_func/src/spectrum_processor_rocm.cpp:267-277, 467-471). */
+typedef enum spx_status {
+  SPX_OK = 0,
+  SPX_ERR_INVALID_ARG = 1,   /* null pointer, size mismatch, unsupported size */
+  SPX_ERR_CUDA = 2,          /* a CUDA runtime call or launch failed */
+  SPX_ERR_OUT_OF_MEMORY = 3, /* device allocation failed ("doesn't fit") */
+  SPX_ERR_UNSUPPORTED = 4,   /* valid request this build does not implement */
+  SPX_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+  SPX_ERR_NO_DEVICE = 6      /* no CUDA device / wrong device ordinal */
+} spx_status;
+
+/* One spectral maximum, 32 bytes; identical layout to antenna_fft::MaxValue
+ * (include/spectrum/types/spectrum_result_types.hpp:34-43).  phase is in
+ * DEGREES, refined_frequency = (index + freq_offset) * fs / nFFT. */
+typedef struct spx_max_value {
+  uint32_t index;
+  float real;
+  float imag;
+  float magnitude;
+  float phase;
+  float freq_offset;
+  float refined_frequency;
+  uint32_t pad;
+} spx_max_value;
+
+/* Window applied to the n_point input samples before zero padding.
+ * NONE..BLACKMAN match fft_processor::WindowType
+ * (include/spectrum/types/window_type.hpp:26-31) with the (n_point-1)
+ * denominator of pad_data_windowed (fft_processor_kernels_rocm.hpp:84-115);
+ * BLACKMAN_HARRIS (4-term, same denominator) has no reference counterpart. */
+enum spx_window {
+  SPX_WINDOW_NONE = 0,
+  SPX_WINDOW_HANN = 1,
+  SPX_WINDOW_HAMMING = 2,
+  SPX_WINDOW_BLACKMAN = 3,
+  SPX_WINDOW_BLACKMAN_HARRIS = 4
+};
+
+/* Output of spx_fft.  COMPLEX: complex64 [beams x nfft], unnormalised.
+ * MAG: float |X|*scale.  MAG2: float |X|^2*scale.  MAGPHASE: interleaved
+ * float2 {|X|, atan2(im,re) radians} (complex_to_mag_phase). */
+enum spx_fft_out {
+  SPX_OUT_COMPLEX = 0,
+  SPX_OUT_MAG = 1,
+  SPX_OUT_MAG2 = 2,
+  SPX_OUT_MAGPHASE = 3
+};
+
+/* Sub-bin refinement written into freq_offset / refined_frequency. */
+enum spx_refine {
+  SPX_REFINE_NONE = 0,      /* delta = 0, f = k*fs/nFFT (compact_maxima) */
+  SPX_REFINE_PARABOLIC = 1  /* 3-point parabola on |X| (post_kernel_one_peak) */
+};
+
+enum spx_peak_mode {
+  SPX_PEAK_ONE = 0,  /* ONE_PEAK: 4 MaxValue per beam */
+  SPX_PEAK_TWO = 1,  /* TWO_PEAKS: 8 MaxValue per beam */
+  SPX_PEAK_ALL = 2,  /* all strict local maxima, compacted */
+  SPX_PEAK_TOPK = 3  /* K largest strict local maxima, magnitude-descending */
+};
+
+/* Peak-search parameters shared by the peak entry points.
+ *  search_start/search_end: ALL/TOPK bin window [start, end); 0 -> 1 and
+ *    0 -> nfft/2, end >= nfft -> nfft-1 (spectrum_processor_rocm.cpp:703-705).
+ *  search_range: ONE/TWO window; 0 -> nfft/4 (spectrum_processor_rocm.cpp:1137-1143);
+ *    bins [0, range/2) and [nfft-range/2, nfft) are searched.
+ *  max_per_beam: ALL: output capacity per beam is
+ *    min((end-start)/2, max_per_beam) (all_maxima_pipeline_rocm.cpp:304-307);
+ *    TOPK: K (1..64).
+ *  thresh_sigma: ALL/TOPK: keep maxima with |X| > noise_median * f(thresh_sigma)
+ *    (see spx_noise_threshold_factor); 0 disables the threshold (reference
+ *    behaviour).
+ *  refine: spx_refine. */
+typedef struct spx_peak_params {
+  uint32_t mode;
+  uint32_t search_start;
+  uint32_t search_end;
+  uint32_t search_range;
+  uint32_t max_per_beam;
+  uint32_t refine;
+  float sample_rate;
+  float thresh_sigma;
+} spx_peak_params;
+
+typedef struct spx_ctx spx_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces the reference's IBackend/GpuContext pair (device + stream). */
+spx_status spx_create(int device, spx_ctx** out);
+spx_status spx_destroy(spx_ctx* ctx);
+/* stream: a cudaStream_t (NULL = legacy default stream). */
+spx_status spx_set_stream(spx_ctx* ctx, void* stream);
+void* spx_get_stream(const spx_ctx* ctx);
+spx_status spx_synchronize(spx_ctx* ctx);
+/* Message of the last failing call on ctx ("" if none).  Valid until the next call. */
+const char* spx_last_error(const spx_ctx* ctx);
+const char* spx_status_string(spx_status status);
+int spx_abi_version(void);
+
+/* ---- sizes -------------------------------------------------------------- */
+/* nextPow2(n) as the reference computes it (fft_processor_rocm.cpp:665-671); 0 -> 1. */
+uint32_t spx_next_pow2(uint32_t n);
+/* Smallest 2^a*3^b >= n (extension for beams of uneven length). */
+uint32_t spx_next_smooth23(uint32_t n);
+/* 1 if this build can transform nfft points (2^a*3^b, 2 <= nfft <= 2^20), else 0. */
+int spx_fft_size_supported(uint32_t nfft);
+/* Resolves the ALL_MAXIMA defaults and returns the per-beam output capacity. */
+spx_status spx_all_maxima_capacity(uint32_t nfft, uint32_t search_start,
+                                   uint32_t search_end, uint32_t max_per_beam,
+                                   uint32_t* start_out, uint32_t* end_out,
+                                   uint32_t* cap_out);
+/* Threshold multiplier applied to the per-beam noise median for thresh_sigma s:
+ * (sqrt(pi/2) + s*sqrt(2 - pi/2)) / sqrt(2 ln 2), i.e. mean + s*std of a
+ * Rayleigh-distributed noise magnitude expressed through its median. */
+float spx_noise_threshold_factor(float thresh_sigma);
+
+/* ---- FFT ---------------------------------------------------------------- */
+/* Batched forward C2C FFT with window and zero padding.
+ *  d_in : complex64 [beams x n_point] (device)
+ *  nfft : >= n_point, 2^a*3^b; samples n_point..nfft-1 are zero
+ *  out_mode / scale: spx_fft_out; scale multiplies MAG and MAG2 (inv_n), ignored otherwise
+ *  d_out: [beams x nfft] of complex64 / float / float / float2 */
+spx_status spx_fft(spx_ctx* ctx, const void* d_in, uint32_t beams,
+                   uint32_t n_point, uint32_t nfft, uint32_t window,
+                   uint32_t out_mode, float scale, void* d_out);
+
+/* ---- magnitude / phase -------------------------------------------------- */
+/* d_out[i] = |d_in[i]| * inv_n (squared: |d_in[i]|^2 * inv_n), count complex64 elements. */
+spx_status spx_magnitude(spx_ctx* ctx, const void* d_in, float* d_out,
+                         uint64_t count, float inv_n, int squared);
+/* d_out[i] = {|d_in[i]|, atan2(im, re)} (radians), interleaved float2. */
+spx_status spx_mag_phase(spx_ctx* ctx, const void* d_in, void* d_out,
+                         uint64_t count);
+
+/* ---- peak search on a spectrum ------------------------------------------ */
+/* ONE_PEAK / TWO_PEAKS on a complex spectrum [beams x nfft]; writes 4 or 8
+ * MaxValue per beam to d_out (post_kernel_one_peak / post_kernel_two_peaks). */
+spx_status spx_peaks_one_two(spx_ctx* ctx, const void* d_fft, uint32_t beams,
+                             uint32_t nfft, uint32_t search_range,
+                             float sample_rate, int two_peaks,
+                             spx_max_value* d_out);
+
+/* All local maxima: detect -> scan -> compact.
+ *  d_mag: float |X| [beams x nfft], or NULL to compute |X| from d_fft
+ *  d_fft: complex64 [beams x nfft] (re/im/phase of each maximum)
+ *  d_out: [beams x cap] (cap from spx_all_maxima_capacity)
+ *  d_counts: [beams], the UNTRUNCATED number of maxima per beam. */
+spx_status spx_all_maxima(spx_ctx* ctx, const float* d_mag, const void* d_fft,
+                          uint32_t beams, uint32_t nfft,
+                          const spx_peak_params* params,
+                          spx_max_value* d_out, uint32_t* d_counts);
+
+/* Top-K strict local maxima in [start, end), ordered by |X| descending, ties
+ * by lower bin; d_out [beams x K], d_counts [beams] = number written (<= K). */
+spx_status spx_topk(spx_ctx* ctx, const float* d_mag, const void* d_fft,
+                    uint32_t beams, uint32_t nfft,
+                    const spx_peak_params* params, spx_max_value* d_out,
+                    uint32_t* d_counts);
+
+/* ---- fused: raw samples -> peaks ---------------------------------------- */
+/* Window + zero-pad + FFT + |X| + peak search in one pass; the spectrum never
+ * goes to device memory.  params->mode selects ONE/TWO/ALL/TOPK with the
+ * layouts of spx_peaks_one_two / spx_all_maxima / spx_topk.  d_counts may be
+ * NULL for ONE/TWO. */
+spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
+                         uint32_t n_point, uint32_t nfft, uint32_t window,
+                         const spx_peak_params* params, spx_max_value* d_out,
+                         uint32_t* d_counts);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* SPX_H_ */

@@ -1,0 +1,195 @@
+// fft_core.cuh — the FFT building blocks used by every spectrum kernel.
+//
+// One beam of nfft = C * M points is transformed by a cluster of C CTAs
+// (C = 1 for nfft <= 16384).  Index maps (n = M*n1 + n2, k = k1 + C*k2):
+//
+//   X[k1 + C*k2] = sum_{n2} W_M^{n2 k2} * ( W_N^{n2 k1} * sum_{n1} x[M n1 + n2] W_C^{n1 k1} )
+//
+// * cross stage (C > 1): CTA c takes n2 in its slice of [0, M), reads the C
+//   samples x[M n1 + n2] straight from device memory (window and zero
+//   padding applied on load), does the C-point DFT in registers, applies
+//   W_N^{n2 k1} and stores element k1 into the shared memory of CTA k1
+//   (distributed shared memory) at local position n2.
+// * local stage: each CTA runs an M-point Stockham FFT (auto-sort, in
+//   place in shared memory, radix 16/9/8/6/4/3/2 in registers) and ends
+//   with Z[k2] = X[c + C*k2] in natural order.
+// * C = 1: the first Stockham pass reads the samples from device memory.
+//
+// Shared memory layout: element i at sw(i) (spx_device.cuh), length
+// padded to a multiple of 16.  Twiddles are FP32 values of FP64-generated
+// exponentials: tw_local holds, per pass p with radix R and stride Ns,
+// W_{Ns R}^{r k} at [(r-1)*Ns + k]; tw_cross holds W_N^{n2 k1} at
+// [(k1-1)*M + n2].
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "spx_device.cuh"
+#include "spx_geom.h"
+
+namespace spx {
+
+namespace cg = cooperative_groups;
+
+// Butterflies per thread needed by radix R when a thread owns <= EPT points.
+template <int EPT, int R>
+struct PassQ {
+  static constexpr int value = (EPT + R - 1) / R;
+};
+
+// Integer j mod Ns and j - j mod Ns for the runtime stride of a pass.
+SPX_DEV uint32_t mod_ns(uint32_t j, uint32_t Ns) {
+  return ((Ns & (Ns - 1)) == 0) ? (j & (Ns - 1)) : (j % Ns);
+}
+
+// Sample n of a beam: window applied, zero beyond n_point.
+SPX_DEV float2 load_sample(const float2* __restrict__ x, uint32_t n,
+                           uint32_t n_point, const float* __restrict__ win) {
+  float2 a = make_float2(0.f, 0.f);
+  if (n < n_point) {
+    a = __ldg(x + n);
+    if (win) {
+      float w = __ldg(win + n);
+      a.x *= w;
+      a.y *= w;
+    }
+  }
+  return a;
+}
+
+// One in-place Stockham pass over shared memory.  Loads all of a thread's
+// butterflies, synchronises, computes, stores, synchronises.
+template <int R, int Q>
+SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns,
+                       const float2* __restrict__ tw, uint32_t tid, uint32_t T) {
+  const uint32_t B = M / R;
+  float2 v[Q][R];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    if (j < B) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q][r] = s[sw(j + r * B)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    if (j < B) {
+      const uint32_t k = mod_ns(j, Ns);
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(tw + (r - 1) * Ns + k));
+      }
+      Dft<R>::run(v[q]);
+      const uint32_t base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) s[sw(base + r * Ns)] = v[q][r];
+    }
+  }
+  __syncthreads();
+}
+
+// First Stockham pass (Ns = 1) reading the beam's samples from device memory.
+template <int R, int Q>
+SPX_DEV void pass_first_global(float2* s, uint32_t M, const float2* __restrict__ x,
+                               uint32_t n_point, const float* __restrict__ win,
+                               uint32_t tid, uint32_t T) {
+  const uint32_t B = M / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    if (j < B) {
+      float2 v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = load_sample(x, j + r * B, n_point, win);
+      Dft<R>::run(v);
+#pragma unroll
+      for (int r = 0; r < R; ++r) s[sw(j * R + r)] = v[r];
+    }
+  }
+  __syncthreads();
+}
+
+// Cross-CTA stage for a cluster of CR CTAs; CTA `c` handles its slice of n2.
+// Ends with a cluster barrier, after which every CTA holds its M inputs.
+template <int CR>
+SPX_DEV void cross_stage(float2* s, uint32_t c, uint32_t M, const float2* __restrict__ x,
+                         uint32_t n_point, const float* __restrict__ win,
+                         const float2* __restrict__ twc, uint32_t tid, uint32_t T) {
+  cg::cluster_group cluster = cg::this_cluster();
+  float2* dst[CR];
+#pragma unroll
+  for (int k1 = 0; k1 < CR; ++k1) dst[k1] = cluster.map_shared_rank(s, k1);
+  const uint32_t S = (M + CR - 1) / CR;
+  const uint32_t lo = c * S;
+  const uint32_t hi = min(lo + S, M);
+  for (uint32_t n2 = lo + tid; n2 < hi; n2 += T) {
+    float2 v[CR];
+#pragma unroll
+    for (int n1 = 0; n1 < CR; ++n1) v[n1] = load_sample(x, n1 * M + n2, n_point, win);
+    Dft<CR>::run(v);
+    const uint32_t p = sw(n2);
+    dst[0][p] = v[0];
+#pragma unroll
+    for (int k1 = 1; k1 < CR; ++k1) dst[k1][p] = cmul(v[k1], __ldg(twc + (k1 - 1) * M + n2));
+  }
+  cluster.sync();
+}
+
+// Runs the passes p, p+1, ... while they have radix R; returns the next pass.
+template <int R, int EPT>
+SPX_DEV uint32_t run_radix(float2* s, const FftGeom& g, uint32_t p,
+                           const float2* __restrict__ tw_local, uint32_t tid, uint32_t T) {
+  while (p < g.npass && g.radix[p] == R) {
+    pass_smem<R, PassQ<EPT, R>::value>(s, g.M, g.ns[p], tw_local + g.twoff[p], tid, T);
+    ++p;
+  }
+  return p;
+}
+
+// Runs the whole transform of one beam; on return shared memory holds
+// Z[k2] = X[c + C*k2] at sw(k2) and all threads of the CTA are synchronised.
+template <int EPT>
+SPX_DEV void fft_beam(float2* s, const FftGeom& g, uint32_t c, const float2* __restrict__ x,
+                      uint32_t n_point, const float* __restrict__ win,
+                      const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
+                      uint32_t tid, uint32_t T) {
+  uint32_t p0 = 0;
+  if (g.C == 1) {
+    switch (g.radix[0]) {
+      case 16: pass_first_global<16, PassQ<EPT, 16>::value>(s, g.M, x, n_point, win, tid, T); break;
+      case 9: pass_first_global<9, PassQ<EPT, 9>::value>(s, g.M, x, n_point, win, tid, T); break;
+      case 8: pass_first_global<8, PassQ<EPT, 8>::value>(s, g.M, x, n_point, win, tid, T); break;
+      case 6: pass_first_global<6, PassQ<EPT, 6>::value>(s, g.M, x, n_point, win, tid, T); break;
+      case 4: pass_first_global<4, PassQ<EPT, 4>::value>(s, g.M, x, n_point, win, tid, T); break;
+      case 3: pass_first_global<3, PassQ<EPT, 3>::value>(s, g.M, x, n_point, win, tid, T); break;
+      default: pass_first_global<2, PassQ<EPT, 2>::value>(s, g.M, x, n_point, win, tid, T); break;
+    }
+    p0 = 1;
+  } else {
+    switch (g.C) {
+      case 2: cross_stage<2>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      case 3: cross_stage<3>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      case 4: cross_stage<4>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      case 6: cross_stage<6>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      case 8: cross_stage<8>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      case 9: cross_stage<9>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+      default: cross_stage<16>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
+    }
+  }
+  // Passes run as consecutive runs of equal radix in the fixed order the plan
+  // builder emits (8, 16..., 9..., 3, 4, 2); one loop per radix keeps the
+  // register allocation of each pass separate (a switch inside a single pass
+  // loop spills).
+  uint32_t p = p0;
+  p = run_radix<8, EPT>(s, g, p, tw_local, tid, T);
+  p = run_radix<16, EPT>(s, g, p, tw_local, tid, T);
+  p = run_radix<9, EPT>(s, g, p, tw_local, tid, T);
+  p = run_radix<3, EPT>(s, g, p, tw_local, tid, T);
+  p = run_radix<4, EPT>(s, g, p, tw_local, tid, T);
+  p = run_radix<2, EPT>(s, g, p, tw_local, tid, T);
+}
+
+}  // namespace spx

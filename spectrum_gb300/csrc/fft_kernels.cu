@@ -1,0 +1,275 @@
+// fft_kernels.cu — batched windowed, zero-padded C2C FFT with a fused output
+// epilogue (complex / |X| / |X|^2 / {|X|, phase}), plus FFT plan building.
+//
+// Replaces PadDataOp + hipfftExecC2C + MagPhaseOp/MagnitudeOp of the
+// reference (include/spectrum/operations/pad_data_op.hpp:82-133,
+// src/fft_func/src/fft_processor_rocm.cpp:353-361,
+// include/spectrum/operations/magnitude_op.hpp:80-103): the zero padding and
+// the window are generated on load, the epilogue runs on the last pass, so
+// each beam reads its n_point samples once and writes its spectrum once.
+#include <cmath>
+#include <mutex>
+#include <set>
+#include <utility>
+#include <vector>
+
+#include "fft_core.cuh"
+#include "spx_internal.h"
+
+namespace spx {
+
+// ---------------------------------------------------------------------------
+// Kernel: one CTA (C == 1) or one cluster of C CTAs per beam.
+// ---------------------------------------------------------------------------
+template <int EPT>
+__global__ void __launch_bounds__(kMaxLocal / EPT, 1)
+fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+               FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
+               void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  const uint32_t tid = threadIdx.x, T = blockDim.x;
+  uint32_t c = 0, beam = blockIdx.x;
+  if (g.C > 1) {
+    c = cg::this_cluster().block_rank();
+    beam = blockIdx.x / g.C;
+  }
+  const float2* x = in + (size_t)beam * n_point;
+  fft_beam<EPT>(s, g, c, x, n_point, win, tw_local, tw_cross, tid, T);
+
+  const size_t obase = (size_t)beam * g.nfft + c;
+  switch (out_mode) {
+    case SPX_OUT_COMPLEX: {
+      float2* o = reinterpret_cast<float2*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = s[sw(i)];
+      break;
+    }
+    case SPX_OUT_MAG: {
+      float* o = reinterpret_cast<float*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag_rn(s[sw(i)]), scale);
+      break;
+    }
+    case SPX_OUT_MAG2: {
+      float* o = reinterpret_cast<float*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag2_rn(s[sw(i)]), scale);
+      break;
+    }
+    default: {  // SPX_OUT_MAGPHASE
+      float2* o = reinterpret_cast<float2*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) {
+        float2 z = s[sw(i)];
+        o[(size_t)g.C * i] = make_float2(mag_rn(z), atan2f(z.y, z.x));
+      }
+      break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host: geometry and twiddle tables.
+// ---------------------------------------------------------------------------
+bool is_smooth23(uint32_t n) {
+  if (n == 0) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+bool build_geom(uint32_t nfft, FftGeom* g) {
+  if (nfft < 2 || !is_smooth23(nfft)) return false;
+  static const uint32_t kClusters[] = {1, 2, 3, 4, 6, 8, 9, 16};
+  uint32_t C = 0;
+  for (uint32_t c : kClusters) {
+    if (nfft % c == 0 && nfft / c <= kMaxLocal) {
+      C = c;
+      break;
+    }
+  }
+  if (C == 0) return false;
+  FftGeom r{};
+  r.nfft = nfft;
+  r.C = C;
+  r.M = nfft / C;
+  r.Mpad = (r.M + 15u) & ~15u;
+  uint32_t a = 0, b = 0, m = r.M;
+  while (m % 2 == 0) { m /= 2; ++a; }
+  while (m % 3 == 0) { m /= 3; ++b; }
+  std::vector<uint32_t> rad;
+  while (a >= 4) { rad.push_back(16); a -= 4; }
+  uint32_t rem2 = 1u << a;  // 1, 2, 4 or 8
+  if (rem2 == 8) { rad.insert(rad.begin(), 8); rem2 = 1; }
+  while (b >= 2) { rad.push_back(9); b -= 2; }
+  if (b == 1) rad.push_back(3);
+  if (rem2 > 1) rad.push_back(rem2);
+  if (rad.empty()) rad.push_back(1);  // M == 1 cannot happen for nfft >= 2 with C <= nfft/2
+  if (rad.size() > (size_t)kMaxPass) return false;
+  r.npass = (uint32_t)rad.size();
+  uint32_t Ns = 1, off = 0;
+  for (uint32_t p = 0; p < r.npass; ++p) {
+    r.radix[p] = rad[p];
+    r.ns[p] = Ns;
+    r.twoff[p] = off;
+    off += Ns * (rad[p] - 1);
+    Ns *= rad[p];
+  }
+  uint32_t T = (r.M + kEPT - 1) / kEPT;
+  T = ((T + 31u) / 32u) * 32u;
+  if (T < 32) T = 32;
+  if (T > kMaxLocal / kEPT) return false;
+  r.T = T;
+  *g = r;
+  return true;
+}
+
+// exp(-2 pi i m / L) in FP64, rounded to FP32.
+static inline float2 twiddle(uint64_t m, uint64_t L) {
+  m %= L;
+  const double a = -2.0 * M_PI * (double)m / (double)L;
+  return make_float2((float)std::cos(a), (float)std::sin(a));
+}
+
+FftPlan::~FftPlan() {
+  if (d_tw_local) cudaFree(d_tw_local);
+  if (d_tw_cross) cudaFree(d_tw_cross);
+}
+
+spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
+  auto it = ctx->plans.find(nfft);
+  if (it != ctx->plans.end()) {
+    *out = it->second.get();
+    return SPX_OK;
+  }
+  auto plan = std::make_unique<FftPlan>();
+  if (!build_geom(nfft, &plan->g))
+    return fail(ctx, SPX_ERR_INVALID_ARG,
+                "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b, 2..262144)");
+  const FftGeom& g = plan->g;
+  std::vector<float2> twl(std::max<uint32_t>(g.M, 1));
+  for (uint32_t p = 0; p < g.npass; ++p) {
+    const uint32_t R = g.radix[p], Ns = g.ns[p];
+    for (uint32_t r = 1; r < R; ++r)
+      for (uint32_t k = 0; k < Ns; ++k)
+        twl[g.twoff[p] + (r - 1) * Ns + k] = twiddle((uint64_t)r * k, (uint64_t)Ns * R);
+  }
+  cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(twiddles)");
+  e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(twiddles)");
+  if (g.C > 1) {
+    std::vector<float2> twc((size_t)(g.C - 1) * g.M);
+    for (uint32_t k1 = 1; k1 < g.C; ++k1)
+      for (uint32_t n2 = 0; n2 < g.M; ++n2)
+        twc[(size_t)(k1 - 1) * g.M + n2] = twiddle((uint64_t)n2 * k1, g.nfft);
+    e = cudaMalloc(&plan->d_tw_cross, twc.size() * sizeof(float2));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(cross twiddles)");
+    e = cudaMemcpy(plan->d_tw_cross, twc.data(), twc.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(cross twiddles)");
+  }
+  *out = plan.get();
+  ctx->plans.emplace(nfft, std::move(plan));
+  return SPX_OK;
+}
+
+// Window w[n], n < n_point, with the reference's (n_point - 1) denominator
+// (fft_processor_kernels_rocm.hpp:97-110), evaluated in FP64.
+static double window_value(uint32_t window, uint32_t n, uint32_t n_point) {
+  if (n_point < 2) return 1.0;
+  const double th = 2.0 * M_PI * (double)n / (double)(n_point - 1);
+  switch (window) {
+    case SPX_WINDOW_HANN: return 0.5 * (1.0 - std::cos(th));
+    case SPX_WINDOW_HAMMING: return 0.54 - 0.46 * std::cos(th);
+    case SPX_WINDOW_BLACKMAN: return 0.42 - 0.5 * std::cos(th) + 0.08 * std::cos(2.0 * th);
+    case SPX_WINDOW_BLACKMAN_HARRIS:
+      return 0.35875 - 0.48829 * std::cos(th) + 0.14128 * std::cos(2.0 * th) -
+             0.01168 * std::cos(3.0 * th);
+    default: return 1.0;
+  }
+}
+
+spx_status get_window(spx_ctx* ctx, uint32_t window, uint32_t n_point, const float** out) {
+  if (window == SPX_WINDOW_NONE) {
+    *out = nullptr;
+    return SPX_OK;
+  }
+  if (window > SPX_WINDOW_BLACKMAN_HARRIS)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "unknown window type " + std::to_string(window));
+  const uint64_t key = ((uint64_t)window << 32) | n_point;
+  auto it = ctx->windows.find(key);
+  if (it != ctx->windows.end()) {
+    *out = it->second;
+    return SPX_OK;
+  }
+  std::vector<float> w(n_point);
+  for (uint32_t n = 0; n < n_point; ++n) w[n] = (float)window_value(window, n, n_point);
+  float* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, std::max<size_t>(1, n_point) * sizeof(float));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(window)");
+  e = cudaMemcpy(d, w.data(), n_point * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_fail(ctx, e, "cudaMemcpy(window)");
+  }
+  ctx->windows[key] = d;
+  *out = d;
+  return SPX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host: launch.
+// ---------------------------------------------------------------------------
+// Raises the dynamic shared-memory limit and allows clusters of 9 and 16
+// once per (device, kernel).
+cudaError_t configure_kernel(const void* kernel, size_t max_smem) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({dev, kernel})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  done.insert({dev, kernel});
+  return cudaSuccess;
+}
+
+template <typename K>
+static cudaError_t launch_beams(K kernel, const FftGeom& g, uint32_t beams, size_t smem,
+                                cudaStream_t stream, void** args) {
+  cudaError_t e0 = configure_kernel((const void*)kernel, kMaxLocal * sizeof(float2) + 16384);
+  if (e0 != cudaSuccess) return e0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(beams * g.C, 1, 1);
+  cfg.blockDim = dim3(g.T, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  if (g.C > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = g.C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelExC(&cfg, (const void*)kernel, args);
+}
+
+spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
+                          uint32_t beams, uint32_t n_point, const float* d_win,
+                          uint32_t out_mode, float scale, void* d_out) {
+  if (beams == 0) return SPX_OK;
+  FftGeom g = plan.g;
+  const float2* twl = plan.d_tw_local;
+  const float2* twc = plan.d_tw_cross;
+  void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
+                  (void*)&twl,  (void*)&twc,     (void*)&d_out, (void*)&out_mode,
+                  (void*)&scale};
+  const size_t smem = (size_t)g.Mpad * sizeof(float2);
+  cudaError_t e = launch_beams(fft_out_kernel<kEPT>, g, beams, smem, ctx->stream, args);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
+  return SPX_OK;
+}
+
+}  // namespace spx

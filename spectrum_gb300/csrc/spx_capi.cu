@@ -1,0 +1,360 @@
+// spx_capi.cu — the extern "C" boundary (include/spx.h): argument checks,
+// reference defaults, context / scratch management and dispatch to the
+// kernels.  No exception crosses this boundary; every entry point returns an
+// spx_status and records a message retrievable with spx_last_error.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "spx_internal.h"
+
+namespace spx {
+
+spx_status fail(spx_ctx* ctx, spx_status st, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return st;
+}
+
+spx_status cuda_fail(spx_ctx* ctx, cudaError_t e, const char* what) {
+  const spx_status st =
+      (e == cudaErrorMemoryAllocation) ? SPX_ERR_OUT_OF_MEMORY : SPX_ERR_CUDA;
+  return fail(ctx, st, std::string(what) + ": " + cudaGetErrorName(e) + " (" +
+                           cudaGetErrorString(e) + ")");
+}
+
+spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out) {
+  if (bytes == 0) bytes = 256;
+  if (ctx->scratch_bytes[slot] < bytes) {
+    if (ctx->d_scratch[slot]) {
+      cudaFree(ctx->d_scratch[slot]);
+      ctx->d_scratch[slot] = nullptr;
+      ctx->scratch_bytes[slot] = 0;
+    }
+    size_t sz = bytes + bytes / 4;  // headroom so slowly growing sizes do not thrash
+    cudaError_t e = cudaMalloc(&ctx->d_scratch[slot], sz);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(ctx, e, "cudaMalloc(scratch)");
+    }
+    ctx->scratch_bytes[slot] = sz;
+  }
+  *out = ctx->d_scratch[slot];
+  return SPX_OK;
+}
+
+// Makes ctx's device current for the duration of an entry point.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Resolves ALL / TOPK window defaults (spectrum_processor_rocm.cpp:703-705).
+static void resolve_window(uint32_t nfft, uint32_t* start, uint32_t* end) {
+  if (*start == 0) *start = 1;
+  if (*end == 0) *end = nfft / 2;
+  if (*end >= nfft) *end = nfft - 1;
+}
+
+static spx_status peak_common_checks(spx_ctx* ctx, const spx_peak_params* p, uint32_t nfft) {
+  if (!p) return fail(ctx, SPX_ERR_INVALID_ARG, "params is null");
+  if (nfft < 3) return fail(ctx, SPX_ERR_INVALID_ARG, "nfft must be >= 3 for a peak search");
+  if (p->refine > SPX_REFINE_PARABOLIC)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "unknown refine mode " + std::to_string(p->refine));
+  if (!(p->thresh_sigma >= 0.0f) || std::isinf(p->thresh_sigma))
+    return fail(ctx, SPX_ERR_INVALID_ARG, "thresh_sigma must be finite and >= 0");
+  return SPX_OK;
+}
+
+// Per-beam thresholds for thresh_sigma > 0 (else *d_thr = null).
+static spx_status thresholds(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                             uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                             float sigma, const float** d_thr) {
+  *d_thr = nullptr;
+  if (sigma <= 0.0f) return SPX_OK;
+  void* t = nullptr;
+  spx_status st = get_scratch(ctx, kSlotThresh, (size_t)beams * sizeof(float), &t);
+  if (st != SPX_OK) return st;
+  st = launch_noise_threshold(ctx, d_mag, d_fft, beams, nfft, start, end,
+                              spx_noise_threshold_factor(sigma), static_cast<float*>(t));
+  if (st != SPX_OK) return st;
+  *d_thr = static_cast<const float*>(t);
+  return SPX_OK;
+}
+
+}  // namespace spx
+
+using namespace spx;
+
+extern "C" {
+
+int spx_abi_version(void) { return SPX_ABI_VERSION; }
+
+const char* spx_status_string(spx_status s) {
+  switch (s) {
+    case SPX_OK: return "SPX_OK";
+    case SPX_ERR_INVALID_ARG: return "SPX_ERR_INVALID_ARG";
+    case SPX_ERR_CUDA: return "SPX_ERR_CUDA";
+    case SPX_ERR_OUT_OF_MEMORY: return "SPX_ERR_OUT_OF_MEMORY";
+    case SPX_ERR_UNSUPPORTED: return "SPX_ERR_UNSUPPORTED";
+    case SPX_ERR_TIMEOUT: return "SPX_ERR_TIMEOUT";
+    case SPX_ERR_NO_DEVICE: return "SPX_ERR_NO_DEVICE";
+  }
+  return "SPX_ERR_UNKNOWN";
+}
+
+spx_status spx_create(int device, spx_ctx** out) {
+  if (!out) return SPX_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return SPX_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return SPX_ERR_NO_DEVICE;
+  spx_ctx* ctx = new (std::nothrow) spx_ctx();
+  if (!ctx) return SPX_ERR_OUT_OF_MEMORY;
+  ctx->device = device;
+  DeviceGuard g(device);
+  if (!g.ok) {
+    delete ctx;
+    return SPX_ERR_NO_DEVICE;
+  }
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (ctx->sm_count <= 0) ctx->sm_count = 1;
+  cudaError_t e = cudaMalloc(&ctx->d_error, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return e == cudaErrorMemoryAllocation ? SPX_ERR_OUT_OF_MEMORY : SPX_ERR_CUDA;
+  }
+  *out = ctx;
+  return SPX_OK;
+}
+
+spx_status spx_destroy(spx_ctx* ctx) {
+  if (!ctx) return SPX_OK;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->plans.clear();
+    for (auto& kv : ctx->windows) cudaFree(kv.second);
+    for (int i = 0; i < 4; ++i)
+      if (ctx->d_scratch[i]) cudaFree(ctx->d_scratch[i]);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+  }
+  delete ctx;
+  return SPX_OK;
+}
+
+spx_status spx_set_stream(spx_ctx* ctx, void* stream) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return SPX_OK;
+}
+
+void* spx_get_stream(const spx_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+const char* spx_last_error(const spx_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+spx_status spx_synchronize(spx_ctx* ctx) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
+  uint32_t err = 0;
+  e = cudaMemcpy(&err, ctx->d_error, sizeof(err), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "read device error word");
+  if (err) {
+    cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+    return fail(ctx, SPX_ERR_TIMEOUT,
+                "a bounded device-side wait expired (error bits " + std::to_string(err) + ")");
+  }
+  return SPX_OK;
+}
+
+uint32_t spx_next_pow2(uint32_t n) {
+  if (n == 0) return 1;
+  n--;
+  n |= n >> 1;
+  n |= n >> 2;
+  n |= n >> 4;
+  n |= n >> 8;
+  n |= n >> 16;
+  return n + 1;
+}
+
+uint32_t spx_next_smooth23(uint32_t n) {
+  if (n <= 1) return 1;
+  uint64_t best = UINT64_MAX;
+  for (uint64_t p2 = 1; p2 < ((uint64_t)n << 1); p2 <<= 1) {
+    uint64_t v = p2;
+    while (v < n) v *= 3;
+    if (v < best) best = v;
+  }
+  return best > 0xFFFFFFFFull ? 0u : (uint32_t)best;
+}
+
+int spx_fft_size_supported(uint32_t nfft) {
+  FftGeom g;
+  return build_geom(nfft, &g) ? 1 : 0;
+}
+
+spx_status spx_all_maxima_capacity(uint32_t nfft, uint32_t search_start, uint32_t search_end,
+                                   uint32_t max_per_beam, uint32_t* start_out,
+                                   uint32_t* end_out, uint32_t* cap_out) {
+  if (nfft < 3) return SPX_ERR_INVALID_ARG;
+  resolve_window(nfft, &search_start, &search_end);
+  // Unsigned arithmetic as in all_maxima_pipeline_rocm.cpp:304-307.
+  uint32_t half = (uint32_t)(search_end - search_start) / 2u;
+  uint32_t cap = half < max_per_beam ? half : max_per_beam;
+  if (start_out) *start_out = search_start;
+  if (end_out) *end_out = search_end;
+  if (cap_out) *cap_out = cap;
+  return SPX_OK;
+}
+
+float spx_noise_threshold_factor(float thresh_sigma) {
+  const double pi = 3.14159265358979323846;
+  const double s = (double)thresh_sigma;
+  return (float)((std::sqrt(pi / 2.0) + s * std::sqrt(2.0 - pi / 2.0)) /
+                 std::sqrt(2.0 * std::log(2.0)));
+}
+
+spx_status spx_fft(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_t n_point,
+                   uint32_t nfft, uint32_t window, uint32_t out_mode, float scale, void* d_out) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (beams == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft: null device pointer");
+  if (n_point == 0) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft: n_point must be > 0");
+  if (nfft < n_point)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft: nfft must be >= n_point");
+  if (out_mode > SPX_OUT_MAGPHASE)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft: unknown out_mode");
+  DeviceGuard g(ctx->device);
+  const FftPlan* plan = nullptr;
+  spx_status st = get_plan(ctx, nfft, &plan);
+  if (st != SPX_OK) return st;
+  const float* win = nullptr;
+  st = get_window(ctx, window, n_point, &win);
+  if (st != SPX_OK) return st;
+  return launch_fft_out(ctx, *plan, static_cast<const float2*>(d_in), beams, n_point, win,
+                        out_mode, scale, d_out);
+}
+
+spx_status spx_magnitude(spx_ctx* ctx, const void* d_in, float* d_out, uint64_t count,
+                         float inv_n, int squared) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (count == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_magnitude: null pointer");
+  DeviceGuard g(ctx->device);
+  return launch_magnitude(ctx, static_cast<const float2*>(d_in), d_out, count, inv_n, squared);
+}
+
+spx_status spx_mag_phase(spx_ctx* ctx, const void* d_in, void* d_out, uint64_t count) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (count == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_mag_phase: null pointer");
+  DeviceGuard g(ctx->device);
+  return launch_mag_phase(ctx, static_cast<const float2*>(d_in), static_cast<float2*>(d_out),
+                          count);
+}
+
+spx_status spx_peaks_one_two(spx_ctx* ctx, const void* d_fft, uint32_t beams, uint32_t nfft,
+                             uint32_t search_range, float sample_rate, int two_peaks,
+                             spx_max_value* d_out) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (beams == 0) return SPX_OK;
+  if (!d_fft || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_peaks_one_two: null pointer");
+  if (nfft < 2) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_peaks_one_two: nfft must be >= 2");
+  if (search_range == 0) search_range = nfft / 4;
+  if (search_range < 2 || search_range > nfft)
+    return fail(ctx, SPX_ERR_INVALID_ARG,
+                "spx_peaks_one_two: search_range must be in [2, nfft] (got " +
+                    std::to_string(search_range) + ")");
+  DeviceGuard g(ctx->device);
+  return launch_one_two(ctx, static_cast<const float2*>(d_fft), beams, nfft, search_range,
+                        sample_rate, two_peaks, d_out);
+}
+
+spx_status spx_all_maxima(spx_ctx* ctx, const float* d_mag, const void* d_fft, uint32_t beams,
+                          uint32_t nfft, const spx_peak_params* params, spx_max_value* d_out,
+                          uint32_t* d_counts) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  spx_status st = peak_common_checks(ctx, params, nfft);
+  if (st != SPX_OK) return st;
+  if (beams == 0) return SPX_OK;
+  if (!d_fft || !d_counts)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_all_maxima: fft_data and counts are required");
+  uint32_t start = 0, end = 0, cap = 0;
+  spx_all_maxima_capacity(nfft, params->search_start, params->search_end, params->max_per_beam,
+                          &start, &end, &cap);
+  if (cap > 0 && !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_all_maxima: out is null");
+  DeviceGuard g(ctx->device);
+  const float* thr = nullptr;
+  st = thresholds(ctx, d_mag, static_cast<const float2*>(d_fft), beams, nfft, start, end,
+                  params->thresh_sigma, &thr);
+  if (st != SPX_OK) return st;
+  return launch_all_maxima(ctx, d_mag, static_cast<const float2*>(d_fft), beams, nfft, start,
+                           end, cap, params->sample_rate, params->refine, thr, d_out, d_counts);
+}
+
+spx_status spx_topk(spx_ctx* ctx, const float* d_mag, const void* d_fft, uint32_t beams,
+                    uint32_t nfft, const spx_peak_params* params, spx_max_value* d_out,
+                    uint32_t* d_counts) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  spx_status st = peak_common_checks(ctx, params, nfft);
+  if (st != SPX_OK) return st;
+  const uint32_t K = params->max_per_beam;
+  if (K < 1 || K > 32) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_topk: K must be in [1, 32]");
+  if (beams == 0) return SPX_OK;
+  if (!d_fft || !d_out || !d_counts)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_topk: null pointer");
+  uint32_t start = params->search_start, end = params->search_end;
+  resolve_window(nfft, &start, &end);
+  DeviceGuard g(ctx->device);
+  const float* thr = nullptr;
+  st = thresholds(ctx, d_mag, static_cast<const float2*>(d_fft), beams, nfft, start, end,
+                  params->thresh_sigma, &thr);
+  if (st != SPX_OK) return st;
+  return launch_topk(ctx, d_mag, static_cast<const float2*>(d_fft), beams, nfft, start, end, K,
+                     params->sample_rate, params->refine, thr, d_out, d_counts);
+}
+
+spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_t n_point,
+                         uint32_t nfft, uint32_t window, const spx_peak_params* params,
+                         spx_max_value* d_out, uint32_t* d_counts) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (!params) return fail(ctx, SPX_ERR_INVALID_ARG, "params is null");
+  if (beams == 0) return SPX_OK;
+  if (params->mode > SPX_PEAK_TOPK)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "unknown peak mode " + std::to_string(params->mode));
+  DeviceGuard g(ctx->device);
+  void* spec = nullptr;
+  spx_status st =
+      get_scratch(ctx, kSlotSpectrum, (size_t)beams * nfft * sizeof(float2), &spec);
+  if (st != SPX_OK) return st;
+  st = spx_fft(ctx, d_in, beams, n_point, nfft, window, SPX_OUT_COMPLEX, 1.0f, spec);
+  if (st != SPX_OK) return st;
+  switch (params->mode) {
+    case SPX_PEAK_ONE:
+    case SPX_PEAK_TWO:
+      return spx_peaks_one_two(ctx, spec, beams, nfft, params->search_range,
+                               params->sample_rate, params->mode == SPX_PEAK_TWO, d_out);
+    case SPX_PEAK_ALL:
+      return spx_all_maxima(ctx, nullptr, spec, beams, nfft, params, d_out, d_counts);
+    default:
+      return spx_topk(ctx, nullptr, spec, beams, nfft, params, d_out, d_counts);
+  }
+}
+
+}  // extern "C"

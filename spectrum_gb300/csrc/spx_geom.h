@@ -1,0 +1,27 @@
+// spx_geom.h — FFT geometry passed by value to the kernels.
+#pragma once
+
+#include <stdint.h>
+
+namespace spx {
+
+constexpr int kMaxPass = 12;
+constexpr uint32_t kMaxLocal = 16384;   // points per CTA (one local FFT)
+constexpr int kEPT = 32;                // points held per thread per pass
+
+// nfft = C * M.  The M-point local FFT runs npass Stockham passes; pass p
+// has radix radix[p], input stride ns[p] (product of earlier radices) and
+// its twiddles at tw_local + twoff[p].
+struct FftGeom {
+  uint32_t nfft;
+  uint32_t C;       // CTAs per beam (cluster size)
+  uint32_t M;       // local FFT length
+  uint32_t Mpad;    // M rounded up to a multiple of 16 (shared-memory elements)
+  uint32_t T;       // threads per CTA
+  uint32_t npass;
+  uint32_t radix[kMaxPass];
+  uint32_t ns[kMaxPass];
+  uint32_t twoff[kMaxPass];
+};
+
+}  // namespace spx

@@ -1,0 +1,95 @@
+// spx_internal.h — host-side state shared by the translation units of the
+// spectrum_gb300 library (not installed; the public boundary is spx.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <memory>
+#include <string>
+
+#include "spx.h"
+#include "spx_geom.h"
+
+namespace spx {
+
+// Device-resident FFT plan for one nfft.
+struct FftPlan {
+  FftGeom g{};
+  float2* d_tw_local = nullptr;  // M - 1 entries (>= 1 allocated)
+  float2* d_tw_cross = nullptr;  // (C - 1) * M entries, or null when C == 1
+  ~FftPlan();
+};
+
+// Fills g for nfft; returns false when nfft is not a supported single-pass size.
+bool build_geom(uint32_t nfft, FftGeom* g);
+bool is_smooth23(uint32_t n);
+
+// Error word bits written by kernels into spx_ctx::d_error.
+constexpr uint32_t kErrLookbackTimeout = 1u;
+
+}  // namespace spx
+
+struct spx_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  std::string last_error;
+  std::map<uint32_t, std::unique_ptr<spx::FftPlan>> plans;
+  std::map<uint64_t, float*> windows;  // (window << 32 | n_point) -> table
+  // Grow-on-demand device scratch, one buffer per slot (see spx::Slot).
+  void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[4] = {0, 0, 0, 0};
+  uint32_t* d_error = nullptr;         // device error word (kErr* bits)
+  uint32_t epoch = 0;                  // lookback status epoch
+};
+
+namespace spx {
+
+// Records msg as the context's last error and returns st.
+spx_status fail(spx_ctx* ctx, spx_status st, const std::string& msg);
+// Maps a CUDA error to SPX_ERR_CUDA / SPX_ERR_OUT_OF_MEMORY with a message.
+spx_status cuda_fail(spx_ctx* ctx, cudaError_t e, const char* what);
+
+// Cached plan / window table (created on first use on the context's device).
+spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out);
+spx_status get_window(spx_ctx* ctx, uint32_t window, uint32_t n_point, const float** out);
+// Scratch slots: buffers that must stay valid at the same time use different slots.
+enum Slot : int {
+  kSlotWork = 0,    // look-back status words, tickets, histograms
+  kSlotThresh = 1,  // per-beam noise thresholds
+  kSlotSpectrum = 2 // intermediate spectra of composed (non-fused) calls
+};
+// Ensures at least `bytes` in `slot`; returns its device pointer.  Growing a
+// slot frees the old buffer (cudaFree waits for the device first).
+spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
+
+// Kernel launchers (fft_kernels.cu, peak_kernels.cu).
+spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
+                          uint32_t beams, uint32_t n_point, const float* d_win,
+                          uint32_t out_mode, float scale, void* d_out);
+spx_status launch_magnitude(spx_ctx* ctx, const float2* d_in, float* d_out,
+                            uint64_t count, float inv_n, int squared);
+spx_status launch_mag_phase(spx_ctx* ctx, const float2* d_in, float2* d_out,
+                            uint64_t count);
+spx_status launch_one_two(spx_ctx* ctx, const float2* d_fft, uint32_t beams,
+                          uint32_t nfft, uint32_t search_range, float fs,
+                          int two_peaks, spx_max_value* d_out);
+// All local maxima (detect + decoupled-lookback scan + compact); thr may be
+// null (no threshold) or hold one threshold per beam.
+spx_status launch_all_maxima(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                             uint32_t beams, uint32_t nfft, uint32_t start,
+                             uint32_t end, uint32_t cap, float fs, uint32_t refine,
+                             const float* d_thr, spx_max_value* d_out,
+                             uint32_t* d_counts);
+spx_status launch_topk(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                       uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                       uint32_t k, float fs, uint32_t refine, const float* d_thr,
+                       spx_max_value* d_out, uint32_t* d_counts);
+// Per-beam noise threshold: median estimate of |X| over [start, end) times factor.
+spx_status launch_noise_threshold(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                                  uint32_t beams, uint32_t nfft, uint32_t start,
+                                  uint32_t end, float factor, float* d_thr);
+
+}  // namespace spx

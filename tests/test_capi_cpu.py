@@ -1,0 +1,89 @@
+"""CPU-only checks of the C ABI: the library loads, exports every symbol that
+include/spx.h declares, and its host-only helpers follow the reference's
+size rules.  No kernel is launched."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "spx.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(spx_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from spectrum_gb300 import _build
+    if not _build.LIB.exists():
+        _build.build()
+    from spectrum_gb300 import _capi
+    return _capi.lib
+
+
+def test_every_declared_symbol_is_exported_and_bound(lib):
+    from spectrum_gb300 import _capi
+    names = _declared_symbols()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in spx.h but not exported"
+        assert n in _capi.PROTOTYPES, f"{n} has no ctypes prototype"
+    assert set(_capi.PROTOTYPES) == set(names)
+
+
+def test_abi_version_and_status_strings(lib):
+    assert lib.spx_abi_version() == 1
+    assert lib.spx_status_string(0) == b"SPX_OK"
+    assert lib.spx_status_string(5) == b"SPX_ERR_TIMEOUT"
+
+
+@pytest.mark.parametrize("n,expect", [(0, 1), (1, 1), (1000, 1024), (1024, 1024), (65537, 131072)])
+def test_next_pow2(lib, n, expect):
+    assert lib.spx_next_pow2(n) == expect
+
+
+def test_next_smooth23_matches_oracle(lib):
+    from oracle import spectrum_oracle as orc
+    for n in list(range(1, 3000)) + [99999, 100000, 98305, 59049, 1 << 20]:
+        assert lib.spx_next_smooth23(n) == orc.next_smooth23(n), n
+
+
+def test_fft_size_support(lib):
+    for n in (2, 3, 8, 4096, 13122, 59049, 104976, 131072, 262144):
+        assert lib.spx_fft_size_supported(n) == 1, n
+    for n in (0, 1, 5, 1000, 524289):
+        assert lib.spx_fft_size_supported(n) == 0, n
+
+
+@pytest.mark.parametrize("nfft,start,end,maxpb", [
+    (1024, 0, 0, 1000), (1024, 5, 2000, 10), (4096, 3000, 100, 1000), (131072, 0, 0, 1000), (8, 1, 2, 5)])
+def test_all_maxima_capacity_matches_reference_rule(lib, nfft, start, end, maxpb):
+    from oracle import spectrum_oracle as orc
+    from spectrum_gb300 import _capi
+    assert _capi.all_maxima_capacity(nfft, start, end, maxpb) == orc.all_maxima_capacity(nfft, start, end, maxpb)
+
+
+def test_noise_threshold_factor(lib):
+    from oracle import spectrum_oracle as orc
+    for s in (0.0, 3.0, 6.0, 10.5):
+        assert lib.spx_noise_threshold_factor(s) == float(orc.noise_threshold_factor(s))
+    assert abs(lib.spx_noise_threshold_factor(6.0) - 4.4024) < 1e-3
+
+
+def test_create_without_gpu_reports_no_device(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert lib.spx_create(0, C.byref(h)) == 6  # SPX_ERR_NO_DEVICE
+    assert not h.value
+
+
+def test_null_context_is_invalid_argument(lib):
+    assert lib.spx_fft(None, None, 1, 1, 1, 0, 0, 1.0, None) == 1
+    assert lib.spx_destroy(None) == 0
+    assert lib.spx_last_error(None) == b""

@@ -1,0 +1,101 @@
+"""GPU parity of the batched FFT (window + zero padding + epilogues) and of the
+magnitude kernels against the oracle (numpy pocketfft FP32 / FP64).
+
+Tolerances: spectra within 1e-5 of the beam's largest |X| (FP32 reference and
+FP64 reference alike); |X| and |X|^2 outputs bit-exact against the same
+formula applied to the kernel's own complex output; phase within 4e-6 rad.
+"""
+import numpy as np
+import pytest
+
+from oracle import spectrum_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+FFT_TOL = 1e-5
+
+# (nfft, n_point, window): every cluster size (1, 2, 3, 4, 6, 8, 9, 16 CTAs per
+# beam), every radix, zero padding and the four windows.
+FFT_CASES = [
+    (2, 2, 0), (3, 3, 0), (4, 3, 0), (6, 5, 1), (8, 8, 0), (9, 9, 2), (12, 7, 0), (16, 10, 3),
+    (64, 64, 0), (243, 200, 1), (1024, 1000, 1), (1152, 1152, 0), (2187, 2000, 4),
+    (4096, 4096, 1), (6561, 6561, 0), (13122, 13000, 2), (13824, 13824, 0), (16384, 16384, 1),
+    (17496, 17000, 0), (19683, 19683, 0), (32768, 20000, 1), (52488, 52000, 0),
+    (65536, 65536, 3), (69984, 69000, 1), (104976, 100000, 1), (131072, 65536, 1),
+    (59049, 59049, 0), (262144, 262144, 0),
+]
+
+
+def _signal(beams, n, seed):
+    rng = np.random.default_rng(seed)
+    return ((rng.standard_normal((beams, n)) + 1j * rng.standard_normal((beams, n))) /
+            np.sqrt(2)).astype(np.complex64)
+
+
+def _max_rel(a, b):
+    scale = np.abs(b).max(axis=-1, keepdims=True)
+    return float((np.abs(a - b) / scale).max())
+
+
+@pytest.mark.parametrize("nfft,n_point,win", FFT_CASES)
+def test_fft_complex_matches_pocketfft(spx, cuda, nfft, n_point, win):
+    import torch
+    beams = 3 if nfft <= 65536 else 2
+    x = _signal(beams, n_point, nfft + n_point)
+    got = spx.fft(torch.from_numpy(x).to(cuda), nfft, window=win).cpu().numpy()
+    ref32 = orc.fft_fp32(x, nfft, win)
+    ref64 = orc.fft_fp64(x, nfft, win)
+    e32 = _max_rel(got, ref32)
+    e64 = _max_rel(got, ref64)
+    assert e32 < FFT_TOL, f"vs FP32 pocketfft: {e32:.3e}"
+    assert e64 < FFT_TOL, f"vs FP64 pocketfft: {e64:.3e}"
+
+
+@pytest.mark.parametrize("nfft,n_point", [(4096, 4000), (131072, 65536), (13122, 13122)])
+def test_fft_epilogues_consistent(spx, cuda, nfft, n_point):
+    """MAG / MAG2 / MAGPHASE come from the same transform as COMPLEX."""
+    import torch
+    x = torch.from_numpy(_signal(2, n_point, 7)).to(cuda)
+    z = spx.fft(x, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    m = spx.fft(x, nfft, window=spx.WINDOW_HANN, out="mag", scale=0.25).cpu().numpy()
+    m2 = spx.fft(x, nfft, window=spx.WINDOW_HANN, out="mag2", scale=0.5).cpu().numpy()
+    mp = spx.fft(x, nfft, window=spx.WINDOW_HANN, out="magphase").cpu().numpy()
+    np.testing.assert_array_equal(m, orc.magnitude(z, 0.25))
+    np.testing.assert_array_equal(m2, orc.magnitude(z, 0.5, squared=True))
+    np.testing.assert_array_equal(mp[..., 0], orc.mag_rn(z))
+    np.testing.assert_allclose(mp[..., 1], np.arctan2(z.imag, z.real), rtol=0, atol=4e-6)
+
+
+@pytest.mark.parametrize("count,offset", [(1, 0), (7, 0), (1 << 20, 0), (1001, 1), (12345, 0)])
+@pytest.mark.parametrize("squared", [False, True])
+def test_magnitude_kernel_bit_exact(spx, cuda, count, offset, squared):
+    """ComplexToMagPhase::ProcessMagnitude semantics, including odd counts and
+    an input not aligned to 16 bytes (scalar path)."""
+    import torch
+    z = _signal(1, count + offset, count)[0]
+    zt = torch.from_numpy(z).to(cuda)[offset:]
+    inv_n = orc.inv_n_from_norm(-1.0, count)
+    got = spx.magnitude(zt, inv_n=inv_n, squared=squared).cpu().numpy()
+    np.testing.assert_array_equal(got, orc.magnitude(z[offset:], inv_n, squared))
+
+
+def test_magnitude_known_values(spx, cuda):
+    """3-4-5 triangle, zero, tiny values (tests/test_complex_to_mag_phase_rocm.hpp:239-259)."""
+    import torch
+    z = np.array([3 + 4j, 0, 1e-6 + 1e-6j, -3 - 4j], np.complex64)
+    got = spx.magnitude(torch.from_numpy(z).to(cuda)).cpu().numpy()
+    np.testing.assert_array_equal(got[[0, 1, 3]], np.float32([5, 0, 5]))
+    assert abs(got[2] - np.float32(np.sqrt(2e-12))) < 1e-12
+    mp = spx.mag_phase(torch.from_numpy(z).to(cuda)).cpu().numpy()
+    np.testing.assert_allclose(mp[:, 1], np.arctan2(z.imag, z.real), atol=4e-6)
+
+
+def test_fft_rejects_bad_sizes(spx, cuda):
+    import torch
+    x = torch.zeros((1, 100), dtype=torch.complex64, device=cuda)
+    with pytest.raises(ValueError):
+        spx.fft(x, 50)           # nfft < n_point
+    with pytest.raises(ValueError):
+        spx.fft(x, 1000)         # 1000 = 2^3 * 5^3 is not 2^a 3^b
+    with pytest.raises(ValueError):
+        spx.fft(x, 1 << 20)      # beyond the single-pass limit
