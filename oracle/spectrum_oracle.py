@@ -253,16 +253,26 @@ def _write_peak4(f: np.ndarray, nfft: int, ci: int, fs: float, mirror: bool) -> 
     return out
 
 
+_BITREV8 = np.array([int(f"{i:08b}"[::-1], 2) for i in range(256)], np.int64)
+
+
 def _argmax_ref_order(vals: np.ndarray) -> int | None:
-    """Argmax with the reference reduction's tie order (256 strided threads,
-    first strict maximum per thread, lower thread id on ties).  Returns the
-    offset into vals, or None when no value is a number."""
+    """Argmax with the reference reduction's tie order.
+
+    post_kernel_one_peak scans a range with 256 threads (thread lid visits
+    offsets lid, lid+256, ... keeping its FIRST strict maximum), then reduces
+    local[lid] with local[lid+stride] for stride = 128, 64, ..., 1, keeping
+    local[lid] on ties (fft_kernel_sources_rocm.hpp:151-192).  The last merge
+    (stride 1) prefers even lids, the one before prefers lid bit 1 = 0, and so
+    on: among equal maxima the winner has the smallest bit-reversed lid
+    (8 bits), then the smallest offset.  Returns the offset, or None when no
+    value is a number."""
     ok = ~np.isnan(vals)
     if not ok.any():
         return None
     m = np.max(vals[ok])
     t = np.nonzero(vals == m)[0]
-    key = (t % 256) * (1 << 24) + (t // 256)
+    key = _BITREV8[t % 256] * (1 << 24) + (t // 256)
     return int(t[np.argmin(key)])
 
 

@@ -124,17 +124,22 @@ SPX_DEV uint64_t lane_max_u64(uint64_t v) {
 // ---------------------------------------------------------------------------
 // Argmax key reproducing the reference's reduction order: a range is scanned
 // by 256 threads, thread `lid` visiting offsets lid, lid+256, ... and keeping
-// its first strict maximum; the tree then keeps the lower lid on ties.  So
-// among equal magnitudes the winner has the smallest (offset mod 256), then
-// the smallest offset.  NaN never wins (key 0).
+// its first strict maximum; the shared-memory tree then merges local[lid]
+// with local[lid + stride] for stride = 128 ... 1, keeping local[lid] on ties
+// (fft_kernel_sources_rocm.hpp:151-192).  The last merge prefers even lids,
+// the one before lid bit 1 = 0, and so on, so among equal magnitudes the
+// winner has the smallest 8-bit-reversed lid, then the smallest offset.
+// The key orders exactly that way under an unsigned max; NaN never wins (0).
 SPX_DEV uint64_t one_two_key(float mag, uint32_t t) {
   if (!(mag >= 0.0f)) return 0ull;
-  const uint32_t low = ~(((t & 255u) << 24) | ((t >> 8) & 0xFFFFFFu));
+  const uint32_t rev = __brev(t & 255u) & 0xFF000000u;  // bit-reversed lid in the top byte
+  const uint32_t low = ~(rev | ((t >> 8) & 0xFFFFFFu));
   return ((uint64_t)__float_as_uint(mag) << 32) | low;
 }
 SPX_DEV uint32_t one_two_offset(uint64_t key) {
   const uint32_t low = ~(uint32_t)key;
-  return ((low & 0xFFFFFFu) << 8) | (low >> 24);
+  const uint32_t lid = __brev(low & 0xFF000000u);  // undo the reversal
+  return ((low & 0xFFFFFFu) << 8) | lid;
 }
 
 // Writes the 4 MaxValue of one peak (interpolated, left, center, right)
