@@ -46,6 +46,8 @@ def _parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-beams", type=int, default=0)
+    ap.add_argument("--profile", action="store_true",
+                    help="device steps only (warmup + steps), no timing report; for ncu captures")
     return ap.parse_args()
 
 
@@ -216,6 +218,11 @@ def run_gpu(args):
                                         C.c_void_p(counts.data_ptr())))
 
     ctx.bind_stream(stream)
+    if args.profile:
+        for i in range(args.warmup + args.steps):
+            step(i)
+        torch.cuda.synchronize()
+        return
     for i in range(max(args.warmup, 3)):
         step(i)
     torch.cuda.synchronize()

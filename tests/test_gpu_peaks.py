@@ -122,8 +122,8 @@ def test_all_maxima_threshold_and_refine(spx, cuda, refine, sigma):
     np.testing.assert_array_equal(counts, rcounts)
     for b in range(4):
         assert_maxvalues_equal(got[b], ref[b], n=int(rcounts[b]))
-    if sigma == 6.0:
-        assert (rcounts >= 6).all() and (rcounts < 40).all()
+    if sigma == 6.0:  # planted lines inside [1, nfft/2) survive, noise maxima do not
+        assert (rcounts >= 1).all() and (rcounts < 20).all()
 
 
 # ---- TOP-K -----------------------------------------------------------------------
