@@ -1,18 +1,19 @@
 // fft_core.cuh — the FFT building blocks used by every spectrum kernel.
 //
-// One beam of nfft = C * M points is transformed by a cluster of C CTAs
-// (C = 1 for nfft <= 16384).  Index maps (n = M*n1 + n2, k = k1 + C*k2):
+// One beam of nfft = C * M points is transformed by C CTAs (C = 1 for
+// nfft <= 16384).  Index maps (n = M*n1 + n2, k = k1 + C*k2):
 //
 //   X[k1 + C*k2] = sum_{n2} W_M^{n2 k2} * ( W_N^{n2 k1} * sum_{n1} x[M n1 + n2] W_C^{n1 k1} )
 //
 // * cross stage (C > 1): CTA c takes n2 in its slice of [0, M), reads the C
 //   samples x[M n1 + n2] straight from device memory (window and zero
 //   padding applied on load), does the C-point DFT in registers, applies
-//   W_N^{n2 k1} and stores element k1 into the shared memory of CTA k1
-//   (distributed shared memory) at local position n2.
-// * local stage: each CTA runs an M-point Stockham FFT (auto-sort, in
-//   place in shared memory, radix 16/9/8/6/4/3/2 in registers) and ends
-//   with Z[k2] = X[c + C*k2] in natural order.
+//   W_N^{n2 k1} and writes element k1 to row k1 of its cluster's exchange
+//   slot in device memory (L2-resident).
+// * local stage: after a cluster barrier CTA k1 runs an M-point Stockham
+//   FFT over row k1 (first pass reading device memory, the others in place
+//   in shared memory, radix 16/9/8/4/3/2 in registers) and ends with
+//   Z[k2] = X[k1 + C*k2] in natural order.
 // * C = 1: the first Stockham pass reads the samples from device memory.
 //
 // Shared memory layout: element i at sw(i) (spx_device.cuh), length
@@ -91,11 +92,24 @@ SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns,
   __syncthreads();
 }
 
-// First Stockham pass (Ns = 1) reading the beam's samples from device memory.
-template <int R, int Q>
-SPX_DEV void pass_first_global(float2* s, uint32_t M, const float2* __restrict__ x,
-                               uint32_t n_point, const float* __restrict__ win,
-                               uint32_t tid, uint32_t T) {
+// Loads sample n of a beam (window, zero padding) through the read-only path.
+struct SampleLoader {
+  const float2* __restrict__ x;
+  uint32_t n_point;
+  const float* __restrict__ win;
+  SPX_DEV float2 operator()(uint32_t n) const { return load_sample(x, n, n_point, win); }
+};
+
+// Loads element n of a row written earlier in the same launch by other CTAs
+// (the cluster exchange slot): L2-coherent loads, never the read-only path.
+struct ExchangeLoader {
+  const float2* row;
+  SPX_DEV float2 operator()(uint32_t n) const { return __ldcg(row + n); }
+};
+
+// First Stockham pass (Ns = 1) reading its inputs from device memory.
+template <int R, int Q, typename Load>
+SPX_DEV void pass_first_global(float2* s, uint32_t M, const Load& load, uint32_t tid, uint32_t T) {
   const uint32_t B = M / R;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -103,7 +117,7 @@ SPX_DEV void pass_first_global(float2* s, uint32_t M, const float2* __restrict__
     if (j < B) {
       float2 v[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = load_sample(x, j + r * B, n_point, win);
+      for (int r = 0; r < R; ++r) v[r] = load(j + r * B);
       Dft<R>::run(v);
 #pragma unroll
       for (int r = 0; r < R; ++r) s[sw(j * R + r)] = v[r];
@@ -112,30 +126,41 @@ SPX_DEV void pass_first_global(float2* s, uint32_t M, const float2* __restrict__
   __syncthreads();
 }
 
-// Cross-CTA stage for a cluster of CR CTAs; CTA `c` handles its slice of n2.
-// Ends with a cluster barrier, after which every CTA holds its M inputs.
+template <int EPT, typename Load>
+SPX_DEV void first_pass_dispatch(float2* s, const FftGeom& g, const Load& load, uint32_t tid,
+                                 uint32_t T) {
+  switch (g.radix[0]) {
+    case 16: pass_first_global<16, PassQ<EPT, 16>::value>(s, g.M, load, tid, T); break;
+    case 9: pass_first_global<9, PassQ<EPT, 9>::value>(s, g.M, load, tid, T); break;
+    case 8: pass_first_global<8, PassQ<EPT, 8>::value>(s, g.M, load, tid, T); break;
+    case 6: pass_first_global<6, PassQ<EPT, 6>::value>(s, g.M, load, tid, T); break;
+    case 4: pass_first_global<4, PassQ<EPT, 4>::value>(s, g.M, load, tid, T); break;
+    case 3: pass_first_global<3, PassQ<EPT, 3>::value>(s, g.M, load, tid, T); break;
+    default: pass_first_global<2, PassQ<EPT, 2>::value>(s, g.M, load, tid, T); break;
+  }
+}
+
+// Cross-CTA stage through device memory: CTA `c` computes the CR-point DFTs
+// of its slice of n2, applies W_N^{n2 k1} and writes element k1 to
+// slot[k1*M + n2] (L2-resident exchange slot of its cluster).  The caller
+// separates this from the reads of the slot with a cluster barrier.
 template <int CR>
-SPX_DEV void cross_stage(float2* s, uint32_t c, uint32_t M, const float2* __restrict__ x,
-                         uint32_t n_point, const float* __restrict__ win,
-                         const float2* __restrict__ twc, uint32_t tid, uint32_t T) {
-  cg::cluster_group cluster = cg::this_cluster();
-  float2* dst[CR];
-#pragma unroll
-  for (int k1 = 0; k1 < CR; ++k1) dst[k1] = cluster.map_shared_rank(s, k1);
+SPX_DEV void cross_stage_exchange(float2* __restrict__ slot, uint32_t c, uint32_t M,
+                                  const SampleLoader& load, const float2* __restrict__ twc,
+                                  uint32_t tid, uint32_t T) {
   const uint32_t S = (M + CR - 1) / CR;
   const uint32_t lo = c * S;
   const uint32_t hi = min(lo + S, M);
   for (uint32_t n2 = lo + tid; n2 < hi; n2 += T) {
     float2 v[CR];
 #pragma unroll
-    for (int n1 = 0; n1 < CR; ++n1) v[n1] = load_sample(x, n1 * M + n2, n_point, win);
+    for (int n1 = 0; n1 < CR; ++n1) v[n1] = load(n1 * M + n2);
     Dft<CR>::run(v);
-    const uint32_t p = sw(n2);
-    dst[0][p] = v[0];
+    __stcg(slot + n2, v[0]);
 #pragma unroll
-    for (int k1 = 1; k1 < CR; ++k1) dst[k1][p] = cmul(v[k1], __ldg(twc + (k1 - 1) * M + n2));
+    for (int k1 = 1; k1 < CR; ++k1)
+      __stcg(slot + (size_t)k1 * M + n2, cmul(v[k1], __ldg(twc + (k1 - 1) * M + n2)));
   }
-  cluster.sync();
 }
 
 // Runs the passes p, p+1, ... while they have radix R; returns the next pass.
@@ -149,40 +174,13 @@ SPX_DEV uint32_t run_radix(float2* s, const FftGeom& g, uint32_t p,
   return p;
 }
 
-// Runs the whole transform of one beam; on return shared memory holds
-// Z[k2] = X[c + C*k2] at sw(k2) and all threads of the CTA are synchronised.
+// Runs local passes p0.. of the plan.  Passes run as consecutive runs of
+// equal radix in the fixed order the plan builder emits (8, 16..., 9..., 3,
+// 4, 2); one loop per radix keeps the register allocation of each pass
+// separate (a switch inside a single pass loop spills).
 template <int EPT>
-SPX_DEV void fft_beam(float2* s, const FftGeom& g, uint32_t c, const float2* __restrict__ x,
-                      uint32_t n_point, const float* __restrict__ win,
-                      const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
-                      uint32_t tid, uint32_t T) {
-  uint32_t p0 = 0;
-  if (g.C == 1) {
-    switch (g.radix[0]) {
-      case 16: pass_first_global<16, PassQ<EPT, 16>::value>(s, g.M, x, n_point, win, tid, T); break;
-      case 9: pass_first_global<9, PassQ<EPT, 9>::value>(s, g.M, x, n_point, win, tid, T); break;
-      case 8: pass_first_global<8, PassQ<EPT, 8>::value>(s, g.M, x, n_point, win, tid, T); break;
-      case 6: pass_first_global<6, PassQ<EPT, 6>::value>(s, g.M, x, n_point, win, tid, T); break;
-      case 4: pass_first_global<4, PassQ<EPT, 4>::value>(s, g.M, x, n_point, win, tid, T); break;
-      case 3: pass_first_global<3, PassQ<EPT, 3>::value>(s, g.M, x, n_point, win, tid, T); break;
-      default: pass_first_global<2, PassQ<EPT, 2>::value>(s, g.M, x, n_point, win, tid, T); break;
-    }
-    p0 = 1;
-  } else {
-    switch (g.C) {
-      case 2: cross_stage<2>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      case 3: cross_stage<3>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      case 4: cross_stage<4>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      case 6: cross_stage<6>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      case 8: cross_stage<8>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      case 9: cross_stage<9>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-      default: cross_stage<16>(s, c, g.M, x, n_point, win, tw_cross, tid, T); break;
-    }
-  }
-  // Passes run as consecutive runs of equal radix in the fixed order the plan
-  // builder emits (8, 16..., 9..., 3, 4, 2); one loop per radix keeps the
-  // register allocation of each pass separate (a switch inside a single pass
-  // loop spills).
+SPX_DEV void local_passes(float2* s, const FftGeom& g, uint32_t p0,
+                          const float2* __restrict__ tw_local, uint32_t tid, uint32_t T) {
   uint32_t p = p0;
   p = run_radix<8, EPT>(s, g, p, tw_local, tid, T);
   p = run_radix<16, EPT>(s, g, p, tw_local, tid, T);

@@ -7,6 +7,7 @@
 // include/spectrum/operations/magnitude_op.hpp:80-103): the zero padding and
 // the window are generated on load, the epilogue runs on the last pass, so
 // each beam reads its n_point samples once and writes its spectrum once.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <set>
@@ -19,23 +20,11 @@
 namespace spx {
 
 // ---------------------------------------------------------------------------
-// Kernel: one CTA (C == 1) or one cluster of C CTAs per beam.
+// Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
 // ---------------------------------------------------------------------------
-template <int EPT>
-__global__ void __launch_bounds__(kMaxLocal / EPT, 1)
-fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
-               FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
-               void* __restrict__ out, uint32_t out_mode, float scale) {
-  extern __shared__ float2 s[];
-  const uint32_t tid = threadIdx.x, T = blockDim.x;
-  uint32_t c = 0, beam = blockIdx.x;
-  if (g.C > 1) {
-    c = cg::this_cluster().block_rank();
-    beam = blockIdx.x / g.C;
-  }
-  const float2* x = in + (size_t)beam * n_point;
-  fft_beam<EPT>(s, g, c, x, n_point, win, tw_local, tw_cross, tid, T);
-
+SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
+                          void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
+                          uint32_t T) {
   const size_t obase = (size_t)beam * g.nfft + c;
   switch (out_mode) {
     case SPX_OUT_COMPLEX: {
@@ -65,6 +54,72 @@ fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __r
 }
 
 // ---------------------------------------------------------------------------
+// Kernel for nfft <= 16384: one CTA per beam.
+// ---------------------------------------------------------------------------
+template <int EPT>
+__global__ void __launch_bounds__(kMaxLocal / EPT, 1)
+fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+               FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
+               void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  const uint32_t tid = threadIdx.x, T = blockDim.x;
+  const uint32_t beam = blockIdx.x;
+  first_pass_dispatch<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tid, T);
+  local_passes<EPT>(s, g, 1, tw_local, tid, T);
+  epilogue_out(s, g, 0, beam, out, out_mode, scale, tid, T);
+}
+
+// ---------------------------------------------------------------------------
+// Kernel for nfft > 16384: one cluster of C CTAs per beam.  The cross-CTA
+// exchange goes through device memory instead of distributed shared memory
+// (measured on GB300: an L2 round trip moves ~10 TB/s, DSMEM stores ~2 TB/s):
+// CTA c writes its C-point DFT outputs into the beam's exchange slot, a
+// cluster barrier (release/acquire) publishes them, CTA k1 reads row k1 in
+// its first Stockham pass and then invalidates the row's L2 lines
+// (discard.global.L2), so the slot never costs a DRAM write-back and only
+// the slots of clusters in flight occupy L2.
+// ---------------------------------------------------------------------------
+// Invalidates (without write-back) every 128-byte L2 line lying entirely in
+// [p, p + bytes); lines shared with a neighbouring row are left alone.
+SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_t T) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t lo = (a + 127) & ~(uintptr_t)127;
+  const uintptr_t hi = (a + bytes) & ~(uintptr_t)127;
+  for (uintptr_t x = lo + (uintptr_t)tid * 128; x < hi; x += (uintptr_t)T * 128)
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
+}
+
+template <int EPT>
+__global__ void __launch_bounds__(kMaxLocal / EPT, 1)
+fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+              FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
+              float2* __restrict__ xch, void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t tid = threadIdx.x, T = blockDim.x;
+  const uint32_t c = cl.block_rank();
+  const uint32_t beam = blockIdx.x / g.C;
+  float2* slot = xch + (size_t)beam * g.nfft;
+  const SampleLoader ld{in + (size_t)beam * n_point, n_point, win};
+  switch (g.C) {
+    case 2: cross_stage_exchange<2>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 3: cross_stage_exchange<3>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 4: cross_stage_exchange<4>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 6: cross_stage_exchange<6>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 8: cross_stage_exchange<8>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 9: cross_stage_exchange<9>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    case 12: cross_stage_exchange<12>(slot, c, g.M, ld, tw_cross, tid, T); break;
+    default: cross_stage_exchange<16>(slot, c, g.M, ld, tw_cross, tid, T); break;
+  }
+  cl.sync();
+  const float2* row = slot + (size_t)c * g.M;
+  first_pass_dispatch<EPT>(s, g, ExchangeLoader{row}, tid, T);
+  discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
+  local_passes<EPT>(s, g, 1, tw_local, tid, T);
+  epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
+}
+
+// ---------------------------------------------------------------------------
 // Host: geometry and twiddle tables.
 // ---------------------------------------------------------------------------
 bool is_smooth23(uint32_t n) {
@@ -76,12 +131,13 @@ bool is_smooth23(uint32_t n) {
 
 bool build_geom(uint32_t nfft, FftGeom* g) {
   if (nfft < 2 || !is_smooth23(nfft)) return false;
-  static const uint32_t kClusters[] = {1, 2, 3, 4, 6, 8, 9, 16};
-  uint32_t C = 0;
-  for (uint32_t c : kClusters) {
-    if (nfft % c == 0 && nfft / c <= kMaxLocal) {
-      C = c;
-      break;
+  // C = 1 up to kMaxLocal points; beyond, the smallest cluster whose CTAs
+  // hold <= kPrefLocalCluster points (two CTAs per SM), else <= kMaxLocal.
+  static const uint32_t kClusters[] = {2, 3, 4, 6, 8, 9, 12, 16};
+  uint32_t C = nfft <= kMaxLocal ? 1u : 0u;
+  for (uint32_t lim : {kPrefLocalCluster, kMaxLocal}) {
+    for (uint32_t c : kClusters) {
+      if (C == 0 && nfft % c == 0 && nfft / c <= lim) C = c;
     }
   }
   if (C == 0) return false;
@@ -263,12 +319,24 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   FftGeom g = plan.g;
   const float2* twl = plan.d_tw_local;
   const float2* twc = plan.d_tw_cross;
-  void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
-                  (void*)&twl,  (void*)&twc,     (void*)&d_out, (void*)&out_mode,
-                  (void*)&scale};
   const size_t smem = (size_t)g.Mpad * sizeof(float2);
-  cudaError_t e = launch_beams(fft_out_kernel<kEPT>, g, beams, smem, ctx->stream, args);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
+  cudaError_t e;
+  if (g.C == 1) {
+    void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
+                    (void*)&twl,  (void*)&twc,     (void*)&d_out, (void*)&out_mode,
+                    (void*)&scale};
+    e = launch_beams(fft_out_kernel<kEPT>, g, beams, smem, ctx->stream, args);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
+    return SPX_OK;
+  }
+  void* xch = nullptr;
+  spx_status st = get_scratch(ctx, kSlotExchange, (size_t)beams * g.nfft * sizeof(float2), &xch);
+  if (st != SPX_OK) return st;
+  float2* xchp = static_cast<float2*>(xch);
+  void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
+                  (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};
+  e = launch_beams(fft_xl_kernel<kEPT>, g, beams, smem, ctx->stream, args);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_xl_kernel");
   return SPX_OK;
 }
 

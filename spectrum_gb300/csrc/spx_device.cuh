@@ -163,6 +163,36 @@ struct Dft<9> {
   }
 };
 
+// 12 = 3 x 4: n = 4*n1 + n2 (n1 < 3, n2 < 4), k = k1 + 3*k2, twiddles W12^{n2 k1}.
+template <>
+struct Dft<12> {
+  static SPX_DEV void run(float2* v) {
+    float2 b[4][3];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      b[n2][0] = v[n2];
+      b[n2][1] = v[4 + n2];
+      b[n2][2] = v[8 + n2];
+      dft3(b[n2][0], b[n2][1], b[n2][2]);
+    }
+    b[1][1] = cmul(b[1][1], make_float2(kS3, -0.5f));   // W12^1
+    b[1][2] = cmul(b[1][2], make_float2(0.5f, -kS3));   // W12^2
+    b[2][1] = cmul(b[2][1], make_float2(0.5f, -kS3));   // W12^2
+    b[2][2] = cmul(b[2][2], make_float2(-0.5f, -kS3));  // W12^4
+    b[3][1] = mul_neg_i(b[3][1]);                        // W12^3
+    b[3][2] = make_float2(-b[3][2].x, -b[3][2].y);       // W12^6
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+      float2 a0 = b[0][k1], a1 = b[1][k1], a2 = b[2][k1], a3 = b[3][k1];
+      dft4(a0, a1, a2, a3);
+      v[k1] = a0;
+      v[k1 + 3] = a1;
+      v[k1 + 6] = a2;
+      v[k1 + 9] = a3;
+    }
+  }
+};
+
 // 16 = 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2, twiddles W16^{n2 k1}.
 template <>
 struct Dft<16> {

@@ -59,7 +59,8 @@ spx_status get_window(spx_ctx* ctx, uint32_t window, uint32_t n_point, const flo
 enum Slot : int {
   kSlotWork = 0,    // look-back status words, tickets, histograms
   kSlotThresh = 1,  // per-beam noise thresholds
-  kSlotSpectrum = 2 // intermediate spectra of composed (non-fused) calls
+  kSlotSpectrum = 2, // intermediate spectra of composed (non-fused) calls
+  kSlotExchange = 3  // per-cluster exchange slots of the large-FFT kernels
 };
 // Ensures at least `bytes` in `slot`; returns its device pointer.  Growing a
 // slot frees the old buffer (cudaFree waits for the device first).
