@@ -204,6 +204,26 @@ spx_status spx_topk(spx_ctx* ctx, const float* d_mag, const void* d_fft,
                     const spx_peak_params* params, spx_max_value* d_out,
                     uint32_t* d_counts);
 
+/* All local maxima without any device allocation.  No counterpart in the
+ * reference: it exists for callers that must not call cudaMalloc while they
+ * run (a real-time loop that reserves its memory at start-up, or a host
+ * framework that owns all device memory through its own pool), which
+ * spx_all_maxima cannot serve because it grows a scratch buffer on demand.
+ * Same arguments, layouts and results as spx_all_maxima, except:
+ *  - thresh_sigma must be 0 (SPX_ERR_INVALID_ARG otherwise);
+ *  - beams * ceil((end - start) / 2048) must be <= 32768 (SPX_ERR_INVALID_ARG);
+ *  - its scratch is one fixed 256 KiB device array inside the library, held
+ *    by every GPU that loads the library until exit and shared by all calls:
+ *    calls whose kernels overlap on the GPU race, so order them on one stream;
+ *  - the first call on a device looks the array's address up (once, with that
+ *    device current); make it before any stream capture.
+ * ctx is only used for its stream and error reporting (spx_create allocates
+ * its small state once, before the no-allocation phase). */
+spx_status spx_all_maxima_noalloc(spx_ctx* ctx, const float* d_mag, const void* d_fft,
+                                  uint32_t beams, uint32_t nfft,
+                                  const spx_peak_params* params,
+                                  spx_max_value* d_out, uint32_t* d_counts);
+
 /* ---- fused: raw samples -> peaks ---------------------------------------- */
 /* Window + zero-pad + FFT + |X| + peak search in one pass; the spectrum never
  * goes to device memory.  params->mode selects ONE/TWO/ALL/TOPK with the

@@ -85,6 +85,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_all_maxima": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_topk": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_fft_peaks": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
+    "spx_all_maxima_noalloc": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
 }
 
 

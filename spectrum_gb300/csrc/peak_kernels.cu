@@ -420,6 +420,49 @@ spx_status launch_all_maxima(spx_ctx* ctx, const float* d_mag, const float2* d_f
   return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch all_maxima_kernel");
 }
 
+// Same launch with caller-provided scratch (status words of `tiles` tiles,
+// then one 32-bit ticket); allocates nothing.  Used by the allocation-free
+// entry point (spx_noalloc.cu).
+spx_status launch_all_maxima_in(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                                uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                                uint32_t cap, float fs, uint32_t refine, spx_max_value* d_out,
+                                uint32_t* d_counts, void* scratch, size_t scratch_bytes) {
+  if (beams == 0) return SPX_OK;
+  const uint64_t tiles = all_maxima_tiles(beams, start, end);
+  const size_t status_bytes = ((size_t)tiles * 8 + 255) & ~(size_t)255;
+  if (status_bytes + sizeof(uint32_t) > scratch_bytes)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "all_maxima: scratch too small");
+  AmArgs a{};
+  a.mag = d_mag;
+  a.fft = d_fft;
+  a.thr = nullptr;
+  a.out = reinterpret_cast<MaxValueDev*>(d_out);
+  a.counts = d_counts;
+  a.status = reinterpret_cast<unsigned long long*>(scratch);
+  a.ticket = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + status_bytes);
+  a.err = ctx->d_error;
+  a.nfft = nfft;
+  a.start = start;
+  a.end = end;
+  a.cap = cap;
+  a.tiles_per_beam = (uint32_t)(tiles / beams);
+  a.epoch = 1;
+  a.refine = refine;
+  a.fs = fs;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, status_bytes + sizeof(uint32_t), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(look-back status)");
+  all_maxima_kernel<<<(unsigned)tiles, kAmThreads, 0, ctx->stream>>>(a);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch all_maxima_kernel");
+}
+
+uint64_t all_maxima_tiles(uint32_t beams, uint32_t start, uint32_t end) {
+  const uint32_t span = end > start ? end - start : 0;
+  uint64_t tpb = (span + kAmTile - 1) / kAmTile;
+  if (tpb == 0) tpb = 1;
+  return tpb * beams;
+}
+
 // ---------------------------------------------------------------------------
 // Top-K strict local maxima, one CTA per beam, one sorted list per warp.
 // ---------------------------------------------------------------------------

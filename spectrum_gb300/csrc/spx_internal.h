@@ -84,6 +84,13 @@ spx_status launch_all_maxima(spx_ctx* ctx, const float* d_mag, const float2* d_f
                              uint32_t end, uint32_t cap, float fs, uint32_t refine,
                              const float* d_thr, spx_max_value* d_out,
                              uint32_t* d_counts);
+// Look-back tiles (thread blocks) of one all-maxima launch.
+uint64_t all_maxima_tiles(uint32_t beams, uint32_t start, uint32_t end);
+// launch_all_maxima without threshold, with caller-provided scratch (no allocation).
+spx_status launch_all_maxima_in(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
+                                uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                                uint32_t cap, float fs, uint32_t refine, spx_max_value* d_out,
+                                uint32_t* d_counts, void* scratch, size_t scratch_bytes);
 spx_status launch_topk(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
                        uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
                        uint32_t k, float fs, uint32_t refine, const float* d_thr,
