@@ -129,8 +129,9 @@ bool is_smooth23(uint32_t n) {
   return n == 1;
 }
 
-bool build_geom(uint32_t nfft, FftGeom* g) {
+bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept) {
   if (nfft < 2 || !is_smooth23(nfft)) return false;
+  if (ept != 16 && ept != 32) return false;
   // C = 1 up to kMaxLocal points; beyond, the smallest cluster whose CTAs
   // hold <= kPrefLocalCluster points (two CTAs per SM), else <= kMaxLocal.
   static const uint32_t kClusters[] = {2, 3, 4, 6, 8, 9, 12, 16};
@@ -167,11 +168,12 @@ bool build_geom(uint32_t nfft, FftGeom* g) {
     off += Ns * (rad[p] - 1);
     Ns *= rad[p];
   }
-  uint32_t T = (r.M + kEPT - 1) / kEPT;
+  uint32_t T = (r.M + ept - 1) / ept;
   T = ((T + 31u) / 32u) * 32u;
   if (T < 32) T = 32;
-  if (T > kMaxLocal / kEPT) return false;
+  if (T > kMaxLocal / ept) return false;
   r.T = T;
+  r.ept = ept;
   *g = r;
   return true;
 }
@@ -189,13 +191,16 @@ FftPlan::~FftPlan() {
 }
 
 spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
-  auto it = ctx->plans.find(nfft);
+  auto te = ctx->tuned_ept.find(nfft);
+  const uint32_t ept = te != ctx->tuned_ept.end() ? te->second : (uint32_t)kEPTDefault;
+  const uint64_t key = ((uint64_t)ept << 32) | nfft;
+  auto it = ctx->plans.find(key);
   if (it != ctx->plans.end()) {
     *out = it->second.get();
     return SPX_OK;
   }
   auto plan = std::make_unique<FftPlan>();
-  if (!build_geom(nfft, &plan->g))
+  if (!build_geom(nfft, &plan->g, ept))
     return fail(ctx, SPX_ERR_INVALID_ARG,
                 "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b, 2..262144)");
   const FftGeom& g = plan->g;
@@ -221,7 +226,7 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(cross twiddles)");
   }
   *out = plan.get();
-  ctx->plans.emplace(nfft, std::move(plan));
+  ctx->plans.emplace(key, std::move(plan));
   return SPX_OK;
 }
 
@@ -321,11 +326,13 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   const float2* twc = plan.d_tw_cross;
   const size_t smem = (size_t)g.Mpad * sizeof(float2);
   cudaError_t e;
+  const bool wide = g.ept == 32;
   if (g.C == 1) {
     void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
                     (void*)&twl,  (void*)&twc,     (void*)&d_out, (void*)&out_mode,
                     (void*)&scale};
-    e = launch_beams(fft_out_kernel<kEPT>, g, beams, smem, ctx->stream, args);
+    e = wide ? launch_beams(fft_out_kernel<32>, g, beams, smem, ctx->stream, args)
+             : launch_beams(fft_out_kernel<16>, g, beams, smem, ctx->stream, args);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
     return SPX_OK;
   }
@@ -335,7 +342,8 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   float2* xchp = static_cast<float2*>(xch);
   void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
                   (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};
-  e = launch_beams(fft_xl_kernel<kEPT>, g, beams, smem, ctx->stream, args);
+  e = wide ? launch_beams(fft_xl_kernel<32>, g, beams, smem, ctx->stream, args)
+           : launch_beams(fft_xl_kernel<16>, g, beams, smem, ctx->stream, args);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_xl_kernel");
   return SPX_OK;
 }

@@ -209,6 +209,17 @@ int spx_fft_size_supported(uint32_t nfft) {
   return build_geom(nfft, &g) ? 1 : 0;
 }
 
+spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  FftGeom g;
+  if (!build_geom(nfft, &g, points_per_thread))
+    return fail(ctx, SPX_ERR_INVALID_ARG,
+                "spx_set_fft_tuning: unsupported (nfft, points_per_thread) = (" +
+                    std::to_string(nfft) + ", " + std::to_string(points_per_thread) + ")");
+  ctx->tuned_ept[nfft] = points_per_thread;
+  return SPX_OK;
+}
+
 spx_status spx_all_maxima_capacity(uint32_t nfft, uint32_t search_start, uint32_t search_end,
                                    uint32_t max_per_beam, uint32_t* start_out,
                                    uint32_t* end_out, uint32_t* cap_out) {

@@ -8,7 +8,7 @@ namespace spx {
 constexpr int kMaxPass = 12;
 constexpr uint32_t kMaxLocal = 16384;   // points per CTA (one local FFT)
 constexpr uint32_t kPrefLocalCluster = 8192;  // preferred points per CTA when C > 1 (2 CTAs / SM)
-constexpr int kEPT = 32;                // points held per thread per pass
+constexpr int kEPTDefault = 16;         // points held per thread per pass (16 or 32)
 
 // nfft = C * M.  The M-point local FFT runs npass Stockham passes; pass p
 // has radix radix[p], input stride ns[p] (product of earlier radices) and
@@ -19,6 +19,7 @@ struct FftGeom {
   uint32_t M;       // local FFT length
   uint32_t Mpad;    // M rounded up to a multiple of 16 (shared-memory elements)
   uint32_t T;       // threads per CTA
+  uint32_t ept;     // points per thread (kernel instantiation: 16 or 32)
   uint32_t npass;
   uint32_t radix[kMaxPass];
   uint32_t ns[kMaxPass];
