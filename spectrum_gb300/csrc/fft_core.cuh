@@ -163,6 +163,16 @@ SPX_DEV void cross_stage_exchange(float2* __restrict__ slot, uint32_t c, uint32_
   }
 }
 
+// Invalidates (without write-back) every 128-byte L2 line lying entirely in
+// [p, p + bytes); lines shared with a neighbouring row are left alone.
+SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_t T) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t lo = (a + 127) & ~(uintptr_t)127;
+  const uintptr_t hi = (a + bytes) & ~(uintptr_t)127;
+  for (uintptr_t x = lo + (uintptr_t)tid * 128; x < hi; x += (uintptr_t)T * 128)
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
+}
+
 // Runs the passes p, p+1, ... while they have radix R; returns the next pass.
 template <int R, int EPT>
 SPX_DEV uint32_t run_radix(float2* s, const FftGeom& g, uint32_t p,

@@ -79,16 +79,6 @@ fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __r
 // (discard.global.L2), so the slot never costs a DRAM write-back and only
 // the slots of clusters in flight occupy L2.
 // ---------------------------------------------------------------------------
-// Invalidates (without write-back) every 128-byte L2 line lying entirely in
-// [p, p + bytes); lines shared with a neighbouring row are left alone.
-SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_t T) {
-  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
-  const uintptr_t lo = (a + 127) & ~(uintptr_t)127;
-  const uintptr_t hi = (a + bytes) & ~(uintptr_t)127;
-  for (uintptr_t x = lo + (uintptr_t)tid * 128; x < hi; x += (uintptr_t)T * 128)
-    asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
-}
-
 template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,

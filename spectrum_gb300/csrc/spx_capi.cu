@@ -346,13 +346,46 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
                          spx_max_value* d_out, uint32_t* d_counts) {
   if (!ctx) return SPX_ERR_INVALID_ARG;
   if (!params) return fail(ctx, SPX_ERR_INVALID_ARG, "params is null");
-  if (beams == 0) return SPX_OK;
   if (params->mode > SPX_PEAK_TOPK)
     return fail(ctx, SPX_ERR_INVALID_ARG, "unknown peak mode " + std::to_string(params->mode));
+  if (beams == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: null device pointer");
+  if (n_point == 0 || nfft < n_point)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: need 0 < n_point <= nfft");
   DeviceGuard g(ctx->device);
+  const FftPlan* plan = nullptr;
+  spx_status st = get_plan(ctx, nfft, &plan);
+  if (st != SPX_OK) return st;
+  // Fused single launch (the spectrum stays on chip) for ALL maxima (C == 1,
+  // or C > 1 with a noise threshold) and TOP-K (C == 1).
+  if (params->mode == SPX_PEAK_ALL || params->mode == SPX_PEAK_TOPK) {
+    st = peak_common_checks(ctx, params, nfft);
+    if (st != SPX_OK) return st;
+    if (!d_counts) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: counts is null");
+    const bool all = params->mode == SPX_PEAK_ALL;
+    uint32_t start = params->search_start, end = params->search_end, cap = 0;
+    if (all) {
+      spx_all_maxima_capacity(nfft, start, end, params->max_per_beam, &start, &end, &cap);
+    } else {
+      if (params->max_per_beam < 1 || params->max_per_beam > 32)
+        return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: K must be in [1, 32]");
+      resolve_window(nfft, &start, &end);
+      cap = params->max_per_beam;
+    }
+    const bool thr = params->thresh_sigma > 0.0f;
+    if (fused_supported(plan->g, params->mode) && (!all || plan->g.C == 1 || thr)) {
+      const float* win = nullptr;
+      st = get_window(ctx, window, n_point, &win);
+      if (st != SPX_OK) return st;
+      return launch_fft_peaks(ctx, *plan, static_cast<const float2*>(d_in), beams, n_point, win,
+                              params->mode, start, end, cap, params->sample_rate, params->refine,
+                              thr ? spx_noise_threshold_factor(params->thresh_sigma) : 0.0f,
+                              d_out, d_counts);
+    }
+  }
+  // Composed path: spectrum to device memory, then the peak kernels.
   void* spec = nullptr;
-  spx_status st =
-      get_scratch(ctx, kSlotSpectrum, (size_t)beams * nfft * sizeof(float2), &spec);
+  st = get_scratch(ctx, kSlotSpectrum, (size_t)beams * nfft * sizeof(float2), &spec);
   if (st != SPX_OK) return st;
   st = spx_fft(ctx, d_in, beams, n_point, nfft, window, SPX_OUT_COMPLEX, 1.0f, spec);
   if (st != SPX_OK) return st;

@@ -68,6 +68,18 @@ enum Slot : int {
 // slot frees the old buffer (cudaFree waits for the device first).
 spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
 
+// Raises a kernel's dynamic shared-memory limit (and allows clusters of
+// up to 16) once per (device, kernel).
+cudaError_t configure_kernel(const void* kernel, size_t max_smem);
+
+// Fused FFT + peak search (fft_peaks.cu).
+bool fused_supported(const FftGeom& g, uint32_t mode);
+spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
+                            uint32_t beams, uint32_t n_point, const float* d_win,
+                            uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
+                            float fs, uint32_t refine, float factor, spx_max_value* d_out,
+                            uint32_t* d_counts);
+
 // Kernel launchers (fft_kernels.cu, peak_kernels.cu).
 spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
                           uint32_t beams, uint32_t n_point, const float* d_win,

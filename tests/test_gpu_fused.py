@@ -1,0 +1,112 @@
+"""GPU parity of the fused raw-samples -> peaks kernel (spx_fft_peaks).
+
+The oracle runs on the spectrum spx_fft returns for the same samples; the
+fused kernel never writes that spectrum, so equal peak lists (bit-exact
+indices, counts and fields; phase within 1e-4 degree) also show the fused
+transform computes the same bits as the plain one.
+"""
+import numpy as np
+import pytest
+
+from oracle import spectrum_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+EXACT = ["index", "real", "imag", "magnitude", "freq_offset", "refined_frequency", "pad"]
+
+
+def assert_rows_equal(got, ref, counts):
+    for b in range(len(counts)):
+        n = min(int(counts[b]), ref.shape[1])
+        for f in EXACT:
+            np.testing.assert_array_equal(got[b, :n][f], ref[b, :n][f], err_msg=f"beam {b} field {f}")
+        np.testing.assert_allclose(got[b, :n]["phase"], ref[b, :n]["phase"], atol=1e-4, rtol=0)
+
+
+def _beams(n_beams, n_point, seed, tones=(1, 16)):
+    from spectrum_gb300 import synth
+    bs = synth.make_beams([n_point] * n_beams, tones=tones, snr_db=(0.0, 40.0), seed=seed)
+    return synth.synth_numpy(bs)
+
+
+# nfft -> cluster size: 4096 (1), 16384 (1), 17496 (3), 20736 (3), 32768 (4), 39366 (6),
+# 65536 (8), 59049 (9), 78732 (12), 104976 (16), 131072 (16)
+ALL_CASES = [(4096, 4096, 6), (16384, 16384, 4), (17496, 17000, 3), (32768, 20000, 3),
+             (39366, 39366, 2), (65536, 65536, 2), (59049, 59049, 2), (78732, 78000, 2),
+             (104976, 100000, 2), (131072, 65536, 4)]
+
+
+@pytest.mark.parametrize("nfft,n_point,beams", ALL_CASES)
+@pytest.mark.parametrize("refine", [0, 1])
+def test_fused_all_maxima_thresholded(spx, cuda, nfft, n_point, beams, refine):
+    import torch
+    x = _beams(beams, n_point, nfft + refine)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_ALL, sample_rate=48000.0,
+                                refine=refine, thresh_sigma=6.0)
+    ref, rc = orc.all_maxima(None, spec, nfft, 48000.0, refine=refine, thresh_sigma=6.0)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+    assert rc.min() >= 1
+
+
+@pytest.mark.parametrize("nfft,start,end,cap", [(4096, 0, 0, 1000), (8192, 100, 3000, 64), (2048, 1, 2047, 10)])
+def test_fused_all_maxima_reference_semantics_single_cta(spx, cuda, nfft, start, end, cap):
+    """No threshold (every strict local maximum), C = 1: still one fused launch."""
+    import torch
+    x = _beams(3, nfft, 7)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_NONE, spx.PEAK_ALL, sample_rate=1.0,
+                                search_start=start, search_end=end, max_per_beam=cap)
+    ref, rc = orc.all_maxima(None, spec, nfft, 1.0, start, end, cap)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+
+
+@pytest.mark.parametrize("nfft,k,sigma", [(4096, 5, 0.0), (8192, 8, 6.0), (1024, 32, 0.0), (16384, 8, 3.0)])
+def test_fused_topk_single_cta(spx, cuda, nfft, k, sigma):
+    import torch
+    x = _beams(4, nfft, k)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_TOPK, sample_rate=1.0,
+                                max_per_beam=k, refine=1, thresh_sigma=sigma)
+    ref, rc = orc.topk(None, spec, nfft, 1.0, k, thresh_sigma=sigma)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+
+
+def test_fused_large_workload_properties(spx, cuda):
+    """The benchmark workload's full size (256 x 65536 -> 131072): properties
+    that need no full oracle run — every reported maximum exceeds its
+    neighbours and the per-beam threshold, bins ascend, counts fit the
+    capacity, and a sampled subset of beams matches the oracle exactly."""
+    import torch
+    from spectrum_gb300 import synth
+    bs = synth.workload_large(seed=1, beams=256)
+    xd = synth.synth_torch(bs, device=cuda)
+    nfft = 131072
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_ALL, sample_rate=1.0,
+                                refine=1, thresh_sigma=6.0)
+    got = spx.maxvalues_to_numpy(out)
+    counts = counts.cpu().numpy().astype(np.uint32)
+    assert (counts >= 1).all() and (counts <= out.shape[1]).all()
+    for b in range(256):
+        idx = got[b, : counts[b]]["index"]
+        assert np.all(np.diff(idx.astype(np.int64)) > 0)
+    sample = [0, 17, 128, 255]
+    spec = spx.fft(xd[sample], nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    ref, rc = orc.all_maxima(None, spec, nfft, 1.0, refine=1, thresh_sigma=6.0)
+    np.testing.assert_array_equal(counts[sample], rc)
+    assert_rows_equal(got[sample], ref, rc)
+    # every planted tone (freq in [0, 0.5) cycles/sample) is found within one bin
+    for j, b in enumerate(sample):
+        f = got[b, : counts[b]]["refined_frequency"]
+        fr = np.asarray(bs.freqs[b])
+        for ft, a in zip(bs.freqs[b], bs.amps[b]):
+            others = np.abs(fr - ft)
+            isolated = np.sort(others)[1] > 16.0 / nfft if len(fr) > 1 else True
+            if a >= 0.5 * max(bs.amps[b]) and isolated:
+                assert np.min(np.abs(f - ft)) < 2.0 / nfft
