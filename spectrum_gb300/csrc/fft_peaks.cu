@@ -31,6 +31,7 @@
 namespace spx {
 
 constexpr uint32_t kHist = 4096;  // noise-histogram buckets (exponent + 4 mantissa bits)
+constexpr uint32_t kList = 1024;  // hot bins classified per round (C > 1); >= threads per CTA
 
 struct FusedArgs {
   const float2* in;
@@ -208,19 +209,48 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
 // ---------------------------------------------------------------------------
 // C > 1: bins k = c + C*i; see the file comment.
 // ---------------------------------------------------------------------------
-SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, const FftGeom& g,
-                           uint32_t c, uint32_t beam, const FusedArgs& a) {
+// Exclusive block-wide prefix of one value per thread; returns the prefix and
+// writes the total to *total (all threads).  Uses s_red[0..65].
+SPX_DEV uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_red, uint32_t* total) {
+  const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) s_red[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t nw = T >> 5;
+    uint32_t w = lane < nw ? s_red[lane] : 0u, u = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
+      if (lane >= (uint32_t)o) u += y;
+    }
+    if (lane < nw) s_red[32 + lane] = u - w;
+    if (lane == nw - 1) s_red[64] = u;
+  }
+  __syncthreads();
+  const uint32_t r = s_red[32 + warp] + x - v;
+  *total = s_red[64];
+  __syncthreads();
+  return r;
+}
+
+SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t* shot,
+                           uint32_t* slist, uint32_t list_cap, const FftGeom& g, uint32_t c,
+                           uint32_t beam, const FusedArgs& a) {
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31;
   const uint32_t C = g.C, M = g.M;
   const uint32_t n = a.end > a.start ? a.end - a.start : 0;
-  // own index range with k in [lo_k, hi_k]
-  auto own_i0 = [&](uint32_t lo_k) { return lo_k <= c ? 0u : (lo_k - c + C - 1) / C; };
+  const uint32_t i_start = a.start <= c ? 0u : (a.start - c + C - 1) / C;
   // 1. histogram over [start, end): shared atomics, then one global atomic per used bucket
   uint32_t* gh = a.ghist + (size_t)beam * kHist;
-  for (uint32_t i = own_i0(a.start) + tid; i < M; i += T) {
-    const uint32_t k = c + C * i;
-    if (k >= a.end) break;
+  for (uint32_t i = i_start + tid; i < M; i += T) {
+    if (c + C * i >= a.end) break;
     atomicAdd(&shist[bucket_of(mag_rn(s[sw(i)]))], 1u);
   }
   __syncthreads();
@@ -230,11 +260,10 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, const Ff
   for (uint32_t b = tid; b < kHist; b += T) shist[b] = __ldcg(gh + b);
   __syncthreads();
   const float thr = threshold_from_hist(shist, n, a.factor, s_red);
-  // 2. hot bitmap of own bins with k in [start-1, end]: word w, bit l <-> i = 32w + l
+  // 2. hot bitmap of own bins with k in [start-1, end]: bit l of word w <-> i = 32w + l
   const uint32_t words = (M + 31) / 32;
   uint32_t* gb = a.gbits + (size_t)beam * ((g.nfft + 31) / 32 + C);
-  uint32_t* mybits = gb + (size_t)c * words;
-  const uint32_t klo = a.start > 0 ? a.start - 1 : 0;
+  const uint32_t klo = a.start - 1;  // start >= 1
   for (uint32_t w0 = 0; w0 < words; w0 += T / 32) {
     const uint32_t w = w0 + (tid >> 5);
     const uint32_t i = 32 * w + lane;
@@ -244,92 +273,98 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, const Ff
       if (k >= klo && k <= a.end) hot = !(mag_rn(s[sw(i)]) <= thr);
     }
     const uint32_t bits = __ballot_sync(0xffffffffu, hot);
-    if (w < words && lane == 0) __stcg(mybits + w, bits);
+    if (w < words && lane == 0) __stcg(gb + (size_t)c * words + w, bits);
   }
   cl.sync();
-  // 3. every CTA classifies every hot bin of the beam (hot bins are few):
-  //    maxima bitmap in bin order in shared memory (reuses the histogram).
-  uint32_t* maxbits = shist;  // nfft/32 words <= 4096 (nfft <= 131072)
-  const uint32_t kwords = (g.nfft + 31) / 32;
-  for (uint32_t w = tid; w < kwords; w += T) maxbits[w] = 0;
+  // 3. all hot bitmaps to shared memory; hot bins of the beam in [start, end) to a list
+  const uint32_t cw_total = C * words;
+  for (uint32_t cw = tid; cw < cw_total; cw += T) shot[cw] = __ldcg(gb + cw);
   __syncthreads();
   auto is_hot = [&](uint32_t k) -> bool {
-    const uint32_t cc = k % C, ii = k / C;
-    return (__ldcg(gb + (size_t)cc * words + (ii >> 5)) >> (ii & 31)) & 1u;
+    const uint32_t ii = k / C;
+    return (shot[(k % C) * words + (ii >> 5)] >> (ii & 31)) & 1u;
   };
   auto mag_at = [&](uint32_t k) -> float {
     const uint32_t cc = k % C, ii = k / C;
     const float2* src = cc == c ? s : cl.map_shared_rank(s, cc);
     return mag_rn(src[sw(ii)]);
   };
-  for (uint32_t cw = tid; cw < C * words; cw += T) {
-    uint32_t bits = __ldcg(gb + cw);
-    const uint32_t cc = cw / words, wi = cw % words;
-    while (bits) {
-      const uint32_t l = __ffs(bits) - 1;
-      bits &= bits - 1;
-      const uint32_t k = cc + C * (32 * wi + l);
-      if (k < a.start || k >= a.end) continue;
-      const float v = mag_at(k);
-      if (!(v > thr)) continue;
-      const bool okl = !is_hot(k - 1) || v > mag_at(k - 1);
-      const bool okr = !is_hot(k + 1) || v > mag_at(k + 1);
-      if (okl && okr) atomicOr(&maxbits[k >> 5], 1u << (k & 31));
+  uint32_t* maxbits = shist;  // nfft/32 words, bin order
+  const uint32_t kwords = (g.nfft + 31) / 32;
+  for (uint32_t w = tid; w < kwords; w += T) maxbits[w] = 0;
+  // chunks of T words: gather hot bins, then classify one per thread
+  for (uint32_t cw0 = 0; cw0 < cw_total; cw0 += T) {
+    const uint32_t cw = cw0 + tid;
+    const uint32_t bits = cw < cw_total ? shot[cw] : 0u;
+    uint32_t total = 0;
+    uint32_t off = block_exclusive_scan(__popc(bits), s_red, &total);
+    for (uint32_t t = bits; t; t &= t - 1) {
+      const uint32_t l = __ffs(t) - 1;
+      if (off < list_cap) slist[off] = (cw / words) + C * (32 * (cw % words) + l);
+      ++off;
     }
+    __syncthreads();
+    // list_cap >= T; longer lists are handled in several passes
+    for (uint32_t base = 0; base < total; base += list_cap) {
+      const uint32_t cnt = min(list_cap, total - base);
+      if (base > 0) {  // refill the list with entries [base, base + cnt)
+        __syncthreads();
+        uint32_t o2 = off - __popc(bits);
+        for (uint32_t t = bits; t; t &= t - 1) {
+          const uint32_t l = __ffs(t) - 1;
+          if (o2 >= base && o2 < base + cnt) slist[o2 - base] = (cw / words) + C * (32 * (cw % words) + l);
+          ++o2;
+        }
+        __syncthreads();
+      }
+      for (uint32_t j = tid; j < cnt; j += T) {
+        const uint32_t k = slist[j];
+        if (k < a.start || k >= a.end) continue;
+        const float v = mag_at(k);
+        if (!(v > thr)) continue;
+        const bool okl = !is_hot(k - 1) || v > mag_at(k - 1);
+        const bool okr = !is_hot(k + 1) || v > mag_at(k + 1);
+        if (okl && okr) atomicOr(&maxbits[k >> 5], 1u << (k & 31));
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  // 4. exclusive prefix popcount over the maxima bitmap (bin order)
-  uint32_t* pref = s_red + 128;  // kwords + 1 entries, see smem layout
+  // 4. prefix popcount of the maxima bitmap per 1024-bin block
+  const uint32_t kblocks = (kwords + 31) / 32;
+  uint32_t* pref = s_red + 128;  // kblocks entries
   {
-    const uint32_t per = (kwords + T - 1) / T;
-    uint32_t sum = 0;
-    for (uint32_t j = 0; j < per; ++j) {
-      const uint32_t w = tid * per + j;
-      if (w < kwords) sum += __popc(maxbits[w]);
-    }
-    uint32_t x = sum;
+    // per-block sums: warp-reduce 32 words at a time
+    for (uint32_t blk0 = 0; blk0 < kblocks; blk0 += T / 32) {
+      const uint32_t blk = blk0 + (tid >> 5);
+      const uint32_t w = blk * 32 + lane;
+      uint32_t v = (blk < kblocks && w < kwords) ? __popc(maxbits[w]) : 0u;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= (uint32_t)o) x += y;
-    }
-    if (lane == 31) s_red[tid >> 5] = x;
-    __syncthreads();
-    if (tid < 32) {
-      const uint32_t nw = T >> 5;
-      uint32_t w = tid < nw ? s_red[tid] : 0u, v = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
-        if (tid >= (uint32_t)o) v += y;
-      }
-      if (tid < nw) s_red[32 + tid] = v - w;
-      if (tid == nw - 1) s_red[64] = v;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0 && blk < kblocks) pref[blk] = v;
     }
     __syncthreads();
-    uint32_t run = s_red[32 + (tid >> 5)] + x - sum;
-    for (uint32_t j = 0; j < per; ++j) {
-      const uint32_t w = tid * per + j;
-      if (w < kwords) {
-        pref[w] = run;
-        run += __popc(maxbits[w]);
+    if (tid == 0) {
+      uint32_t run = 0;
+      for (uint32_t blk = 0; blk < kblocks; ++blk) {
+        const uint32_t v = pref[blk];
+        pref[blk] = run;
+        run += v;
       }
+      s_red[64] = run;
     }
     __syncthreads();
   }
   if (c == 0 && tid == 0) a.counts[beam] = s_red[64];
-  // 5. own maxima -> MaxValue at their rank
+  // 5. own maxima -> MaxValue at their rank (own hot bits, one word per thread)
   const float bw = __fdiv_rn(a.fs, (float)g.nfft);
-  for (uint32_t w = 0; w < words; ++w) {
-    uint32_t bits = __ldcg(mybits + w);  // own hot bits (written by this CTA)
-    for (uint32_t b2 = bits; b2; b2 &= b2 - 1) {
-      // distribute the set bits of this word over the threads
-      const uint32_t l = __ffs(b2) - 1;
-      const uint32_t idx = __popc(bits & ((1u << l) - 1u));
-      if (idx % T != tid) continue;
+  for (uint32_t w = tid; w < words; w += T) {
+    for (uint32_t t = shot[(size_t)c * words + w]; t; t &= t - 1) {
+      const uint32_t l = __ffs(t) - 1;
       const uint32_t i = 32 * w + l, k = c + C * i;
       if (k < a.start || k >= a.end || !((maxbits[k >> 5] >> (k & 31)) & 1u)) continue;
-      const uint32_t rank = pref[k >> 5] + __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
+      uint32_t rank = pref[k >> 10];
+      for (uint32_t w2 = (k >> 10) << 5; w2 < (k >> 5); ++w2) rank += __popc(maxbits[w2]);
+      rank += __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
       if (rank < a.cap)
         a.out[(size_t)beam * a.cap + rank] =
             fused_max(k, s[sw(i)], mag_at(k - 1), mag_rn(s[sw(i)]), mag_at(k + 1), bw, a.refine);
@@ -342,9 +377,12 @@ template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_peaks_kernel(FftGeom g, FusedArgs a) {
   extern __shared__ float2 s[];
-  // layout: spectrum [Mpad] | histogram / bitmaps [4096 + 64] u32 | reductions [128 + kwords + 1] u32
+  // layout (u32 after the spectrum): histogram / maxima bitmap [4096 + 64] |
+  // reductions [128 + 128] | hot bitmaps [C * ceil(M/32)] | hot-bin list [kList]
   uint32_t* shist = reinterpret_cast<uint32_t*>(s + g.Mpad);
   uint32_t* s_red = shist + kHist + 64;
+  uint32_t* shot = s_red + 256;
+  uint32_t* slist = shot + g.C * ((g.M + 31) / 32);
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
   if (g.C == 1) {
@@ -375,20 +413,21 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   first_pass_dispatch<EPT>(s, g, ExchangeLoader{row}, tid, T);
   discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
   local_passes<EPT>(s, g, 1, a.tw_local, tid, T);
-  peaks_cluster(s, shist, s_red, g, c, beam, a);
+  peaks_cluster(s, shist, s_red, shot, slist, kList, g, c, beam, a);
 }
 
 // Shared memory of the fused kernel for geometry g.
 static size_t fused_smem(const FftGeom& g) {
-  const size_t kwords = (g.nfft + 31) / 32;
-  return (size_t)g.Mpad * sizeof(float2) + (kHist + 64 + 128 + kwords + 1) * sizeof(uint32_t);
+  const size_t hot = g.C > 1 ? (size_t)g.C * ((g.M + 31) / 32) + kList : 0;
+  return (size_t)g.Mpad * sizeof(float2) + (kHist + 64 + 256 + hot) * sizeof(uint32_t);
 }
 
 bool fused_supported(const FftGeom& g, uint32_t mode) {
   if (mode == SPX_PEAK_TOPK) return g.C == 1;
   if (mode != SPX_PEAK_ALL) return false;
   if ((g.nfft + 31) / 32 > kHist) return false;  // maxima bitmap lives in the histogram area
-  return (kHist % g.T) == 0 && fused_smem(g) <= 227 * 1024;
+  if ((g.nfft + 31) / 32 > 128 * 32) return false;  // block prefix table holds 128 entries
+  return (kHist % g.T) == 0 && g.T <= kList && fused_smem(g) <= 227 * 1024;
 }
 
 spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
