@@ -40,7 +40,7 @@ struct FusedArgs {
   const float2* tw_cross;
   float2* xch;              // exchange slots (C > 1), one per beam
   uint32_t* ghist;          // [beams][4096] per-beam histograms (C > 1), zeroed by the host
-  uint32_t* gbits;          // [beams][nfft/32 + C] hot bitmaps (C > 1)
+  uint32_t* gbits;          // [beams][2][nfft/32 + C] hot / maxima bitmaps (C > 1)
   MaxValueDev* out;
   uint32_t* counts;
   uint32_t n_point, start, end, cap, mode, K, refine;
@@ -262,8 +262,10 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
   const float thr = threshold_from_hist(shist, n, a.factor, s_red);
   // 2. hot bitmap of own bins with k in [start-1, end]: bit l of word w <-> i = 32w + l
   const uint32_t words = (M + 31) / 32;
-  uint32_t* gb = a.gbits + (size_t)beam * ((g.nfft + 31) / 32 + C);
-  const uint32_t klo = a.start - 1;  // start >= 1
+  const size_t beam_words = (size_t)(g.nfft + 31) / 32 + C;
+  uint32_t* gb = a.gbits + (size_t)beam * 2 * beam_words;  // hot bitmaps
+  uint32_t* gm = gb + beam_words;                          // maxima bitmaps
+  const uint32_t klo = a.start - 1;                        // start >= 1
   for (uint32_t w0 = 0; w0 < words; w0 += T / 32) {
     const uint32_t w = w0 + (tid >> 5);
     const uint32_t i = 32 * w + lane;
@@ -276,7 +278,8 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
     if (w < words && lane == 0) __stcg(gb + (size_t)c * words + w, bits);
   }
   cl.sync();
-  // 3. all hot bitmaps to shared memory; hot bins of the beam in [start, end) to a list
+  // 3. classify OWN hot bins; the two neighbours (other CTAs) are read once,
+  //    in parallel over the hot bins, and kept for the refinement.
   const uint32_t cw_total = C * words;
   for (uint32_t cw = tid; cw < cw_total; cw += T) shot[cw] = __ldcg(gb + cw);
   __syncthreads();
@@ -284,90 +287,94 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
     const uint32_t ii = k / C;
     return (shot[(k % C) * words + (ii >> 5)] >> (ii & 31)) & 1u;
   };
-  auto mag_at = [&](uint32_t k) -> float {
-    const uint32_t cc = k % C, ii = k / C;
+  auto remote_mag = [&](uint32_t k) -> float {
+    const uint32_t cc = k % C;
     const float2* src = cc == c ? s : cl.map_shared_rank(s, cc);
-    return mag_rn(src[sw(ii)]);
+    return mag_rn(src[sw(k / C)]);
   };
-  uint32_t* maxbits = shist;  // nfft/32 words, bin order
+  // own hot bins -> slist (i values), in rounds of list_cap
+  uint32_t* mywords = shist;  // own maxima bits (words), reuses the histogram
+  for (uint32_t w = tid; w < words; w += T) mywords[w] = 0;
+  uint32_t per_thread = 0;
+  for (uint32_t w = tid; w < words; w += T) per_thread += __popc(shot[(size_t)c * words + w]);
+  uint32_t total = 0;
+  uint32_t off = block_exclusive_scan(per_thread, s_red, &total);
+  for (uint32_t base = 0; base < total; base += list_cap) {
+    const uint32_t cnt = min(list_cap, total - base);
+    uint32_t o = off;
+    for (uint32_t w = tid; w < words; w += T) {
+      for (uint32_t t = shot[(size_t)c * words + w]; t; t &= t - 1) {
+        if (o >= base && o < base + cnt) slist[o - base] = 32 * w + (__ffs(t) - 1);
+        ++o;
+      }
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < cnt; j += T) {
+      const uint32_t i = slist[j], k = c + C * i;
+      if (k < a.start || k >= a.end) continue;
+      const float v = mag_rn(s[sw(i)]);
+      if (!(v > thr)) continue;
+      // a cold neighbour is <= thr < v; only hot ones are read (rare, remote)
+      const bool hl = is_hot(k - 1), hr = is_hot(k + 1);
+      const float yl = hl ? remote_mag(k - 1) : 0.f;
+      const float yr = hr ? remote_mag(k + 1) : 0.f;
+      if ((!hl || v > yl) && (!hr || v > yr)) atomicOr(&mywords[i >> 5], 1u << (i & 31));
+    }
+    __syncthreads();
+  }
+  for (uint32_t w = tid; w < words; w += T) __stcg(gm + (size_t)c * words + w, mywords[w]);
+  cl.sync();
+  // 4. maxima of the whole beam in bin order, prefix popcount per 1024-bin block
+  uint32_t* maxbits = shot;  // the hot bitmaps are no longer needed: reuse (nfft/32 words)
   const uint32_t kwords = (g.nfft + 31) / 32;
+  __syncthreads();
   for (uint32_t w = tid; w < kwords; w += T) maxbits[w] = 0;
-  // chunks of T words: gather hot bins, then classify one per thread
-  for (uint32_t cw0 = 0; cw0 < cw_total; cw0 += T) {
-    const uint32_t cw = cw0 + tid;
-    const uint32_t bits = cw < cw_total ? shot[cw] : 0u;
-    uint32_t total = 0;
-    uint32_t off = block_exclusive_scan(__popc(bits), s_red, &total);
-    for (uint32_t t = bits; t; t &= t - 1) {
-      const uint32_t l = __ffs(t) - 1;
-      if (off < list_cap) slist[off] = (cw / words) + C * (32 * (cw % words) + l);
-      ++off;
+  __syncthreads();
+  for (uint32_t cw = tid; cw < cw_total; cw += T) {
+    const uint32_t cc = cw / words, wi = cw % words;
+    for (uint32_t t = __ldcg(gm + cw); t; t &= t - 1) {
+      const uint32_t k = cc + C * (32 * wi + (__ffs(t) - 1));
+      atomicOr(&maxbits[k >> 5], 1u << (k & 31));
     }
-    __syncthreads();
-    // list_cap >= T; longer lists are handled in several passes
-    for (uint32_t base = 0; base < total; base += list_cap) {
-      const uint32_t cnt = min(list_cap, total - base);
-      if (base > 0) {  // refill the list with entries [base, base + cnt)
-        __syncthreads();
-        uint32_t o2 = off - __popc(bits);
-        for (uint32_t t = bits; t; t &= t - 1) {
-          const uint32_t l = __ffs(t) - 1;
-          if (o2 >= base && o2 < base + cnt) slist[o2 - base] = (cw / words) + C * (32 * (cw % words) + l);
-          ++o2;
-        }
-        __syncthreads();
-      }
-      for (uint32_t j = tid; j < cnt; j += T) {
-        const uint32_t k = slist[j];
-        if (k < a.start || k >= a.end) continue;
-        const float v = mag_at(k);
-        if (!(v > thr)) continue;
-        const bool okl = !is_hot(k - 1) || v > mag_at(k - 1);
-        const bool okr = !is_hot(k + 1) || v > mag_at(k + 1);
-        if (okl && okr) atomicOr(&maxbits[k >> 5], 1u << (k & 31));
-      }
-    }
-    __syncthreads();
   }
-  // 4. prefix popcount of the maxima bitmap per 1024-bin block
+  __syncthreads();
   const uint32_t kblocks = (kwords + 31) / 32;
-  uint32_t* pref = s_red + 128;  // kblocks entries
-  {
-    // per-block sums: warp-reduce 32 words at a time
-    for (uint32_t blk0 = 0; blk0 < kblocks; blk0 += T / 32) {
-      const uint32_t blk = blk0 + (tid >> 5);
-      const uint32_t w = blk * 32 + lane;
-      uint32_t v = (blk < kblocks && w < kwords) ? __popc(maxbits[w]) : 0u;
+  uint32_t* pref = s_red + 128;  // kblocks <= 128 entries
+  for (uint32_t blk0 = 0; blk0 < kblocks; blk0 += T / 32) {
+    const uint32_t blk = blk0 + (tid >> 5);
+    const uint32_t w = blk * 32 + lane;
+    uint32_t v = (blk < kblocks && w < kwords) ? __popc(maxbits[w]) : 0u;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0 && blk < kblocks) pref[blk] = v;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t run = 0;
-      for (uint32_t blk = 0; blk < kblocks; ++blk) {
-        const uint32_t v = pref[blk];
-        pref[blk] = run;
-        run += v;
-      }
-      s_red[64] = run;
-    }
-    __syncthreads();
+    for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
+    if (lane == 0 && blk < kblocks) pref[blk] = v;
   }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t run = 0;
+    for (uint32_t blk = 0; blk < kblocks; ++blk) {
+      const uint32_t v = pref[blk];
+      pref[blk] = run;
+      run += v;
+    }
+    s_red[64] = run;
+  }
+  __syncthreads();
   if (c == 0 && tid == 0) a.counts[beam] = s_red[64];
-  // 5. own maxima -> MaxValue at their rank (own hot bits, one word per thread)
+  // 5. own maxima -> MaxValue at their rank (neighbour magnitudes for the
+  //    refinement read from the neighbours' CTAs)
   const float bw = __fdiv_rn(a.fs, (float)g.nfft);
   for (uint32_t w = tid; w < words; w += T) {
-    for (uint32_t t = shot[(size_t)c * words + w]; t; t &= t - 1) {
-      const uint32_t l = __ffs(t) - 1;
-      const uint32_t i = 32 * w + l, k = c + C * i;
-      if (k < a.start || k >= a.end || !((maxbits[k >> 5] >> (k & 31)) & 1u)) continue;
+    for (uint32_t t = mywords[w]; t; t &= t - 1) {
+      const uint32_t i = 32 * w + (__ffs(t) - 1), k = c + C * i;
       uint32_t rank = pref[k >> 10];
       for (uint32_t w2 = (k >> 10) << 5; w2 < (k >> 5); ++w2) rank += __popc(maxbits[w2]);
       rank += __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
-      if (rank < a.cap)
-        a.out[(size_t)beam * a.cap + rank] =
-            fused_max(k, s[sw(i)], mag_at(k - 1), mag_rn(s[sw(i)]), mag_at(k + 1), bw, a.refine);
+      if (rank < a.cap) {
+        const float2 z = s[sw(i)];
+        const bool par = a.refine == SPX_REFINE_PARABOLIC;
+        const float yl = par ? remote_mag(k - 1) : 0.f, yr = par ? remote_mag(k + 1) : 0.f;
+        a.out[(size_t)beam * a.cap + rank] = fused_max(k, z, yl, mag_rn(z), yr, bw, a.refine);
+      }
     }
   }
   cl.sync();  // other CTAs may still read this CTA's shared memory
@@ -457,7 +464,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   if (g.C > 1) {
     const size_t xch_bytes = (size_t)beams * g.nfft * sizeof(float2);
     const size_t hist_bytes = (size_t)beams * kHist * sizeof(uint32_t);
-    const size_t bits_bytes = (size_t)beams * ((g.nfft + 31) / 32 + g.C) * sizeof(uint32_t);
+    const size_t bits_bytes = (size_t)beams * 2 * ((g.nfft + 31) / 32 + g.C) * sizeof(uint32_t);
     void* p = nullptr;
     spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + hist_bytes + bits_bytes + 512, &p);
     if (st != SPX_OK) return st;
