@@ -125,11 +125,7 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
   const uint32_t n = a.end > a.start ? a.end - a.start : 0;
   float thr = -INFINITY;
   if (a.factor > 0.0f) {
-    for (uint32_t k0 = a.start; k0 < a.end; k0 += T) {  // uniform trip count per warp
-      const uint32_t k = k0 + tid;
-      const bool ok = k < a.end;
-      warp_hist_add(shist, ok ? bucket_of(mag_rn(s[sw(k)])) : 0u, ok);
-    }
+    for (uint32_t k = a.start + tid; k < a.end; k += T) atomicAdd(&shist[bucket_of(mag_rn(s[sw(k)]))], 1u);
     __syncthreads();
     thr = threshold_from_hist(shist, n, a.factor, s_red);
   }
@@ -254,11 +250,7 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
   // 1. histogram over [start, end): shared atomics, then one global atomic per used bucket
   uint32_t* gh = a.ghist + (size_t)beam * kHist;
   const uint32_t i_end = a.end <= c ? 0u : min(M, (a.end - c + C - 1) / C);  // first i with k >= end
-  for (uint32_t i0 = i_start; i0 < i_end; i0 += T) {  // uniform trip count per warp
-    const uint32_t i = i0 + tid;
-    const bool ok = i < i_end;
-    warp_hist_add(shist, ok ? bucket_of(mag_rn(s[sw(i)])) : 0u, ok);
-  }
+  for (uint32_t i = i_start + tid; i < i_end; i += T) atomicAdd(&shist[bucket_of(mag_rn(s[sw(i)]))], 1u);
   __syncthreads();
   for (uint32_t b = tid; b < kHist; b += T)
     if (shist[b]) atomicAdd(&gh[b], shist[b]);

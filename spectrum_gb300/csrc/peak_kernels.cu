@@ -573,11 +573,8 @@ noise_hist_kernel(const float* __restrict__ mag, const float2* __restrict__ fft,
   const uint32_t beam = blockIdx.x / tiles_per_beam, t = blockIdx.x % tiles_per_beam;
   const size_t bb = (size_t)beam * nfft;
   const uint32_t lo = start + t * kHistTile, hi = min(lo + kHistTile, end);
-  for (uint32_t b0 = lo; b0 < hi; b0 += blockDim.x) {  // uniform trip count per warp
-    const uint32_t bin = b0 + threadIdx.x;
-    const bool ok = bin < hi;
-    warp_hist_add(h, ok ? noise_bucket(mag_at(mag, fft, bb + bin)) : 0u, ok);
-  }
+  for (uint32_t bin = lo + threadIdx.x; bin < hi; bin += blockDim.x)
+    atomicAdd(&h[noise_bucket(mag_at(mag, fft, bb + bin))], 1u);
   __syncthreads();
   uint32_t* g = hist + (size_t)beam * kHistBins;
   for (uint32_t i = threadIdx.x; i < kHistBins; i += blockDim.x)

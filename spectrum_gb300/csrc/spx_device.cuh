@@ -230,23 +230,6 @@ struct Dft<16> {
   }
 };
 
-// ---- warp-aggregated histogram increment -----------------------------------
-// Adds 1 to h[b] for every active lane with valid = true.  Lanes sharing a
-// bucket are counted with one atomic (noise magnitudes fall into a handful
-// of buckets, so plain per-lane atomics would serialize).  Call from all
-// lanes of the warp (valid = false for lanes without a value).
-SPX_DEV void warp_hist_add(uint32_t* h, uint32_t b, bool valid) {
-  const uint32_t lane = threadIdx.x & 31;
-  uint32_t pending = __ballot_sync(0xffffffffu, valid);
-  while (pending) {
-    const int leader = __ffs(pending) - 1;
-    const uint32_t lb = __shfl_sync(0xffffffffu, b, leader);
-    const uint32_t same = __ballot_sync(0xffffffffu, valid && b == lb) & pending;
-    if (lane == (uint32_t)leader) atomicAdd(&h[lb], (uint32_t)__popc(same));
-    pending &= ~same;
-  }
-}
-
 // ---- MaxValue (32 bytes, the reference's GPU layout) -------------------------
 struct MaxValueDev {
   uint32_t index;
