@@ -16,13 +16,13 @@
 // spx_topk: the same FFT code, |X| = sqrt_rn(re*re + im*im), the same
 // histogram-median threshold and the same comparisons.
 //
-// C > 1 (the beam's bins k = c + C*i are spread over the cluster): exact and
-// sparse.  Bin k is "hot" when !(|X[k]| <= T) (NaN counts as hot, so it
-// compares exactly like the reference).  A maximum is hot, and a cold
-// neighbour is <= T < |X[k]|, so only hot neighbours need comparing.  Hot
-// bitmaps go through device memory, the few magnitudes a CTA needs from other
-// CTAs come from their shared memory (DSMEM), ranks come from a prefix
-// popcount over the beam's maxima bitmap in bin order.
+// C > 1 (the beam's bins k = c + C*i are spread over the cluster): after the
+// cluster barrier that completes the beam's noise histogram every spectrum is
+// final, so each CTA tests its bins above the threshold (few) against both
+// neighbours read from the neighbours' CTAs (distributed shared memory) and
+// keeps their magnitudes for the refinement; maxima bitmaps go through
+// device memory, and after one more barrier every CTA ranks its maxima by a
+// prefix popcount over the beam's maxima bitmap in bin order.
 #include <cuda/atomic>
 
 #include "fft_core.cuh"
@@ -40,7 +40,7 @@ struct FusedArgs {
   const float2* tw_cross;
   float2* xch;              // exchange slots (C > 1), one per beam
   uint32_t* ghist;          // [beams][4096] per-beam histograms (C > 1), zeroed by the host
-  uint32_t* gbits;          // [beams][2][nfft/32 + C] hot / maxima bitmaps (C > 1)
+  uint32_t* gbits;          // [beams][nfft/32 + C] maxima bitmaps (C > 1)
   MaxValueDev* out;
   uint32_t* counts;
   uint32_t n_point, start, end, cap, mode, K, refine;
@@ -247,9 +247,11 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
   const uint32_t C = g.C, M = g.M;
   const uint32_t n = a.end > a.start ? a.end - a.start : 0;
   const uint32_t i_start = a.start <= c ? 0u : (a.start - c + C - 1) / C;
-  // 1. histogram over [start, end): shared atomics, then one global atomic per used bucket
-  uint32_t* gh = a.ghist + (size_t)beam * kHist;
   const uint32_t i_end = a.end <= c ? 0u : min(M, (a.end - c + C - 1) / C);  // first i with k >= end
+  // 1. histogram over [start, end): shared atomics, one global atomic per used bucket.
+  //    After the barrier every CTA's spectrum is final, so DSMEM reads are safe
+  //    until the last barrier below.
+  uint32_t* gh = a.ghist + (size_t)beam * kHist;
   for (uint32_t i = i_start + tid; i < i_end; i += T) atomicAdd(&shist[bucket_of(mag_rn(s[sw(i)]))], 1u);
   __syncthreads();
   for (uint32_t b = tid; b < kHist; b += T)
@@ -258,77 +260,54 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
   for (uint32_t b = tid; b < kHist; b += T) shist[b] = __ldcg(gh + b);
   __syncthreads();
   const float thr = threshold_from_hist(shist, n, a.factor, s_red);
-  // 2. hot bitmap of own bins with k in [start-1, end]: bit l of word w <-> i = 32w + l
-  const uint32_t words = (M + 31) / 32;
-  const size_t beam_words = (size_t)(g.nfft + 31) / 32 + C;
-  uint32_t* gb = a.gbits + (size_t)beam * 2 * beam_words;  // hot bitmaps
-  uint32_t* gm = gb + beam_words;                          // maxima bitmaps
-  const uint32_t klo = a.start - 1;                        // start >= 1
-  for (uint32_t w0 = 0; w0 < words; w0 += T / 32) {
-    const uint32_t w = w0 + (tid >> 5);
-    const uint32_t i = 32 * w + lane;
-    bool hot = false;
-    if (w < words && i < M) {
-      const uint32_t k = c + C * i;
-      if (k >= klo && k <= a.end) hot = !(mag_rn(s[sw(i)]) <= thr);
-    }
-    const uint32_t bits = __ballot_sync(0xffffffffu, hot);
-    if (w < words && lane == 0) __stcg(gb + (size_t)c * words + w, bits);
-  }
-  cl.sync();
-  // 3. classify OWN hot bins; the two neighbours (other CTAs) are read once,
-  //    in parallel over the hot bins, and kept for the refinement.
-  const uint32_t cw_total = C * words;
-  for (uint32_t cw = tid; cw < cw_total; cw += T) shot[cw] = __ldcg(gb + cw);
-  __syncthreads();
-  auto is_hot = [&](uint32_t k) -> bool {
-    const uint32_t ii = k / C;
-    return (shot[(k % C) * words + (ii >> 5)] >> (ii & 31)) & 1u;
-  };
-  auto remote_mag = [&](uint32_t k) -> float {
+  // Bins above the threshold's bucket bound the beam's hot bins; the bound
+  // is the same in every CTA (same histogram), so the choice below is uniform.
+  const uint32_t tb = bucket_of(thr);
+  uint32_t hot_bound = 0;
+  for (uint32_t b = tid; b < kHist; b += T) hot_bound += b >= tb ? shist[b] : 0u;
+  uint32_t hot_total = 0;
+  (void)block_exclusive_scan(hot_bound, s_red, &hot_total);
+  const bool keep_records = hot_total <= list_cap;
+  // 2. classify own hot bins (|X| > thr) against both neighbours, read from
+  //    their CTAs; record (i, y_l, y_r) of the maxima for the output.
+  auto mag_at = [&](uint32_t k) -> float {
     const uint32_t cc = k % C;
     const float2* src = cc == c ? s : cl.map_shared_rank(s, cc);
     return mag_rn(src[sw(k / C)]);
   };
-  // own hot bins -> slist (i values), in rounds of list_cap
-  uint32_t* mywords = shist;  // own maxima bits (words), reuses the histogram
+  const uint32_t words = (M + 31) / 32;
+  uint32_t* mywords = shot;  // own maxima bits, bit l of word w <-> i = 32w + l
+  float* rec = reinterpret_cast<float*>(slist);  // [list_cap][3] = {i, y_l, y_r}
+  uint32_t* s_nrec = s_red + 100;
   for (uint32_t w = tid; w < words; w += T) mywords[w] = 0;
-  uint32_t per_thread = 0;
-  for (uint32_t w = tid; w < words; w += T) per_thread += __popc(shot[(size_t)c * words + w]);
-  uint32_t total = 0;
-  uint32_t off = block_exclusive_scan(per_thread, s_red, &total);
-  for (uint32_t base = 0; base < total; base += list_cap) {
-    const uint32_t cnt = min(list_cap, total - base);
-    uint32_t o = off;
-    for (uint32_t w = tid; w < words; w += T) {
-      for (uint32_t t = shot[(size_t)c * words + w]; t; t &= t - 1) {
-        if (o >= base && o < base + cnt) slist[o - base] = 32 * w + (__ffs(t) - 1);
-        ++o;
+  if (tid == 0) *s_nrec = 0;
+  __syncthreads();
+  for (uint32_t i = i_start + tid; i < i_end; i += T) {
+    const float v = mag_rn(s[sw(i)]);
+    if (!(v > thr)) continue;
+    const uint32_t k = c + C * i;
+    const float yl = mag_at(k - 1), yr = mag_at(k + 1);
+    if (v > yl && v > yr) {
+      atomicOr(&mywords[i >> 5], 1u << (i & 31));
+      if (keep_records) {
+        const uint32_t r = atomicAdd(s_nrec, 1u);
+        rec[3 * r] = __uint_as_float(i);
+        rec[3 * r + 1] = yl;
+        rec[3 * r + 2] = yr;
       }
     }
-    __syncthreads();
-    for (uint32_t j = tid; j < cnt; j += T) {
-      const uint32_t i = slist[j], k = c + C * i;
-      if (k < a.start || k >= a.end) continue;
-      const float v = mag_rn(s[sw(i)]);
-      if (!(v > thr)) continue;
-      // a cold neighbour is <= thr < v; only hot ones are read (rare, remote)
-      const bool hl = is_hot(k - 1), hr = is_hot(k + 1);
-      const float yl = hl ? remote_mag(k - 1) : 0.f;
-      const float yr = hr ? remote_mag(k + 1) : 0.f;
-      if ((!hl || v > yl) && (!hr || v > yr)) atomicOr(&mywords[i >> 5], 1u << (i & 31));
-    }
-    __syncthreads();
   }
+  __syncthreads();
+  const size_t beam_words = (size_t)(g.nfft + 31) / 32 + C;
+  uint32_t* gm = a.gbits + (size_t)beam * beam_words;  // maxima bitmaps of the cluster
   for (uint32_t w = tid; w < words; w += T) __stcg(gm + (size_t)c * words + w, mywords[w]);
   cl.sync();
-  // 4. maxima of the whole beam in bin order, prefix popcount per 1024-bin block
-  uint32_t* maxbits = shot;  // the hot bitmaps are no longer needed: reuse (nfft/32 words)
+  // 3. maxima of the whole beam in bin order, prefix popcount per 1024-bin block
   const uint32_t kwords = (g.nfft + 31) / 32;
-  __syncthreads();
+  uint32_t* maxbits = shist;
   for (uint32_t w = tid; w < kwords; w += T) maxbits[w] = 0;
   __syncthreads();
-  for (uint32_t cw = tid; cw < cw_total; cw += T) {
+  for (uint32_t cw = tid; cw < C * words; cw += T) {
     const uint32_t cc = cw / words, wi = cw % words;
     for (uint32_t t = __ldcg(gm + cw); t; t &= t - 1) {
       const uint32_t k = cc + C * (32 * wi + (__ffs(t) - 1));
@@ -336,46 +315,66 @@ SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t
     }
   }
   __syncthreads();
-  const uint32_t kblocks = (kwords + 31) / 32;
-  uint32_t* pref = s_red + 128;  // kblocks <= 128 entries
+  const uint32_t kblocks = (kwords + 31) / 32;  // <= 128
+  uint32_t* pref = s_red + 128;
   for (uint32_t blk0 = 0; blk0 < kblocks; blk0 += T / 32) {
     const uint32_t blk = blk0 + (tid >> 5);
     const uint32_t w = blk * 32 + lane;
     uint32_t v = (blk < kblocks && w < kwords) ? __popc(maxbits[w]) : 0u;
 #pragma unroll
-    for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0 && blk < kblocks) pref[blk] = v;
   }
   __syncthreads();
-  if (tid == 0) {
-    uint32_t run = 0;
-    for (uint32_t blk = 0; blk < kblocks; ++blk) {
-      const uint32_t v = pref[blk];
-      pref[blk] = run;
-      run += v;
+  if (tid < 32) {  // exclusive scan of <= 128 block sums, 4 per lane
+    uint32_t v[4], sum = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t blk = tid * 4 + j;
+      v[j] = blk < kblocks ? pref[blk] : 0u;
+      sum += v[j];
     }
-    s_red[64] = run;
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (tid >= (uint32_t)o) x += y;
+    }
+    uint32_t run = x - sum;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t blk = tid * 4 + j;
+      if (blk < kblocks) pref[blk] = run;
+      run += v[j];
+    }
+    if (tid == 31) s_red[64] = x;
   }
   __syncthreads();
   if (c == 0 && tid == 0) a.counts[beam] = s_red[64];
-  // 5. own maxima -> MaxValue at their rank (neighbour magnitudes for the
-  //    refinement read from the neighbours' CTAs)
+  // 4. own maxima -> MaxValue at their rank
   const float bw = __fdiv_rn(a.fs, (float)g.nfft);
-  for (uint32_t w = tid; w < words; w += T) {
+  auto write_max = [&](uint32_t i, float yl, float yr) {
+    const uint32_t k = c + C * i;
+    uint32_t rank = pref[k >> 10];
+    for (uint32_t w2 = (k >> 10) << 5; w2 < (k >> 5); ++w2) rank += __popc(maxbits[w2]);
+    rank += __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
+    if (rank < a.cap) {
+      const float2 z = s[sw(i)];
+      a.out[(size_t)beam * a.cap + rank] = fused_max(k, z, yl, mag_rn(z), yr, bw, a.refine);
+    }
+  };
+  if (keep_records) {
+    const uint32_t nrec = *s_nrec;
+    for (uint32_t r = tid; r < nrec; r += T)
+      write_max(__float_as_uint(rec[3 * r]), rec[3 * r + 1], rec[3 * r + 2]);
+    return;  // no DSMEM access after the last barrier
+  }
+  for (uint32_t w = tid; w < words; w += T)
     for (uint32_t t = mywords[w]; t; t &= t - 1) {
       const uint32_t i = 32 * w + (__ffs(t) - 1), k = c + C * i;
-      uint32_t rank = pref[k >> 10];
-      for (uint32_t w2 = (k >> 10) << 5; w2 < (k >> 5); ++w2) rank += __popc(maxbits[w2]);
-      rank += __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
-      if (rank < a.cap) {
-        const float2 z = s[sw(i)];
-        const bool par = a.refine == SPX_REFINE_PARABOLIC;
-        const float yl = par ? remote_mag(k - 1) : 0.f, yr = par ? remote_mag(k + 1) : 0.f;
-        a.out[(size_t)beam * a.cap + rank] = fused_max(k, z, yl, mag_rn(z), yr, bw, a.refine);
-      }
+      write_max(i, mag_at(k - 1), mag_at(k + 1));
     }
-  }
-  cl.sync();  // other CTAs may still read this CTA's shared memory
+  cl.sync();  // (many maxima) other CTAs read this CTA's shared memory above
 }
 
 template <int EPT>
@@ -383,11 +382,11 @@ __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_peaks_kernel(FftGeom g, FusedArgs a) {
   extern __shared__ float2 s[];
   // layout (u32 after the spectrum): histogram / maxima bitmap [4096 + 64] |
-  // reductions [128 + 128] | hot bitmaps [C * ceil(M/32)] | hot-bin list [kList]
+  // reductions [256] | own maxima bits [ceil(M/32)] | maxima records [3 * kList]
   uint32_t* shist = reinterpret_cast<uint32_t*>(s + g.Mpad);
   uint32_t* s_red = shist + kHist + 64;
   uint32_t* shot = s_red + 256;
-  uint32_t* slist = shot + g.C * ((g.M + 31) / 32);
+  uint32_t* slist = shot + (g.M + 31) / 32;
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
   if (g.C == 1) {
@@ -423,7 +422,7 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
 
 // Shared memory of the fused kernel for geometry g.
 static size_t fused_smem(const FftGeom& g) {
-  const size_t hot = g.C > 1 ? (size_t)g.C * ((g.M + 31) / 32) + kList : 0;
+  const size_t hot = g.C > 1 ? (size_t)(g.M + 31) / 32 + 3 * kList : 0;
   return (size_t)g.Mpad * sizeof(float2) + (kHist + 64 + 256 + hot) * sizeof(uint32_t);
 }
 
@@ -462,7 +461,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   if (g.C > 1) {
     const size_t xch_bytes = (size_t)beams * g.nfft * sizeof(float2);
     const size_t hist_bytes = (size_t)beams * kHist * sizeof(uint32_t);
-    const size_t bits_bytes = (size_t)beams * 2 * ((g.nfft + 31) / 32 + g.C) * sizeof(uint32_t);
+    const size_t bits_bytes = (size_t)beams * ((g.nfft + 31) / 32 + g.C) * sizeof(uint32_t);
     void* p = nullptr;
     spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + hist_bytes + bits_bytes + 512, &p);
     if (st != SPX_OK) return st;
