@@ -151,10 +151,13 @@ uint32_t spx_next_pow2(uint32_t n);
 uint32_t spx_next_smooth23(uint32_t n);
 /* 1 if this build can transform nfft points (2^a*3^b, 2 <= nfft <= 2^20), else 0. */
 int spx_fft_size_supported(uint32_t nfft);
-/* Tuning: points each thread holds per FFT pass for transforms of nfft points
- * (16: more resident warps; 32: more work per thread).  No reference
- * counterpart (hipFFT chooses internally); set by the autotuner or by hand. */
-spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread);
+/* Tuning for transforms of nfft points: points each thread holds per pass
+ * (16: more resident warps; 32: more work per thread) and, above 16384
+ * points, the preferred points per CTA of a beam's cluster (1024..16384;
+ * 0 = default 8192: two CTAs per SM).  No reference counterpart (hipFFT
+ * chooses internally); set by the autotuner or by hand. */
+spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread,
+                              uint32_t points_per_cta);
 /* Resolves the ALL_MAXIMA defaults and returns the per-beam output capacity. */
 spx_status spx_all_maxima_capacity(uint32_t nfft, uint32_t search_start,
                                    uint32_t search_end, uint32_t max_per_beam,

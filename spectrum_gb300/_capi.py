@@ -76,7 +76,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_next_pow2": (_u32, [_u32]),
     "spx_next_smooth23": (_u32, [_u32]),
     "spx_fft_size_supported": (_i, [_u32]),
-    "spx_set_fft_tuning": (_i, [_vp, _u32, _u32]),
+    "spx_set_fft_tuning": (_i, [_vp, _u32, _u32, _u32]),
     "spx_all_maxima_capacity": (_i, [_u32, _u32, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "spx_noise_threshold_factor": (_f, [_f]),
     "spx_fft": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, _u32, _f, _vp]),

@@ -119,14 +119,15 @@ bool is_smooth23(uint32_t n) {
   return n == 1;
 }
 
-bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept) {
+bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept, uint32_t pref_local) {
   if (nfft < 2 || !is_smooth23(nfft)) return false;
   if (ept != 16 && ept != 32) return false;
+  if (pref_local < 1024 || pref_local > kMaxLocal) return false;
   // C = 1 up to kMaxLocal points; beyond, the smallest cluster whose CTAs
   // hold <= kPrefLocalCluster points (two CTAs per SM), else <= kMaxLocal.
   static const uint32_t kClusters[] = {2, 3, 4, 6, 8, 9, 12, 16};
   uint32_t C = nfft <= kMaxLocal ? 1u : 0u;
-  for (uint32_t lim : {kPrefLocalCluster, kMaxLocal}) {
+  for (uint32_t lim : {pref_local, kMaxLocal}) {
     for (uint32_t c : kClusters) {
       if (C == 0 && nfft % c == 0 && nfft / c <= lim) C = c;
     }
@@ -181,16 +182,17 @@ FftPlan::~FftPlan() {
 }
 
 spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
-  auto te = ctx->tuned_ept.find(nfft);
-  const uint32_t ept = te != ctx->tuned_ept.end() ? te->second : (uint32_t)kEPTDefault;
-  const uint64_t key = ((uint64_t)ept << 32) | nfft;
+  auto te = ctx->tuning.find(nfft);
+  const uint32_t ept = te != ctx->tuning.end() ? te->second.first : (uint32_t)kEPTDefault;
+  const uint32_t pref = te != ctx->tuning.end() ? te->second.second : kPrefLocalCluster;
+  const uint64_t key = ((uint64_t)ept << 56) | ((uint64_t)pref << 32) | nfft;
   auto it = ctx->plans.find(key);
   if (it != ctx->plans.end()) {
     *out = it->second.get();
     return SPX_OK;
   }
   auto plan = std::make_unique<FftPlan>();
-  if (!build_geom(nfft, &plan->g, ept))
+  if (!build_geom(nfft, &plan->g, ept, pref))
     return fail(ctx, SPX_ERR_INVALID_ARG,
                 "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b, 2..262144)");
   const FftGeom& g = plan->g;

@@ -209,14 +209,17 @@ int spx_fft_size_supported(uint32_t nfft) {
   return build_geom(nfft, &g) ? 1 : 0;
 }
 
-spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread) {
+spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread,
+                              uint32_t points_per_cta) {
   if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (points_per_cta == 0) points_per_cta = kPrefLocalCluster;
   FftGeom g;
-  if (!build_geom(nfft, &g, points_per_thread))
+  if (!build_geom(nfft, &g, points_per_thread, points_per_cta))
     return fail(ctx, SPX_ERR_INVALID_ARG,
-                "spx_set_fft_tuning: unsupported (nfft, points_per_thread) = (" +
-                    std::to_string(nfft) + ", " + std::to_string(points_per_thread) + ")");
-  ctx->tuned_ept[nfft] = points_per_thread;
+                "spx_set_fft_tuning: unsupported (nfft, points_per_thread, points_per_cta) = (" +
+                    std::to_string(nfft) + ", " + std::to_string(points_per_thread) + ", " +
+                    std::to_string(points_per_cta) + ")");
+  ctx->tuning[nfft] = {points_per_thread, points_per_cta};
   return SPX_OK;
 }
 

@@ -24,7 +24,8 @@ struct FftPlan {
 
 // Fills g for nfft with `ept` points per thread (16 or 32); returns false
 // when nfft is not a supported single-pass size.
-bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept = kEPTDefault);
+bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept = kEPTDefault,
+                uint32_t pref_local = kPrefLocalCluster);
 bool is_smooth23(uint32_t n);
 
 // Error word bits written by kernels into spx_ctx::d_error.
@@ -37,8 +38,8 @@ struct spx_ctx {
   cudaStream_t stream = nullptr;
   int sm_count = 0;
   std::string last_error;
-  std::map<uint64_t, std::unique_ptr<spx::FftPlan>> plans;  // (ept << 32 | nfft)
-  std::map<uint32_t, uint32_t> tuned_ept;  // nfft -> points per thread chosen by tuning
+  std::map<uint64_t, std::unique_ptr<spx::FftPlan>> plans;  // (ept, points/CTA, nfft)
+  std::map<uint32_t, std::pair<uint32_t, uint32_t>> tuning;  // nfft -> (points/thread, points/CTA)
   std::map<uint64_t, float*> windows;  // (window << 32 | n_point) -> table
   // Grow-on-demand device scratch, one buffer per slot (see spx::Slot).
   void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
