@@ -154,7 +154,7 @@ int spx_fft_size_supported(uint32_t nfft);
 /* Tuning for transforms of nfft points: points each thread holds per pass
  * (16: more resident warps; 32: more work per thread) and, above 16384
  * points, the preferred points per CTA of a beam's cluster (1024..16384;
- * 0 = default 8192: two CTAs per SM).  No reference counterpart (hipFFT
+ * 0 = default 16384: one CTA per SM; 8192 allows two).  No reference counterpart (hipFFT
  * chooses internally); set by the autotuner or by hand. */
 spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread,
                               uint32_t points_per_cta);
@@ -240,6 +240,40 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
                          uint32_t n_point, uint32_t nfft, uint32_t window,
                          const spx_peak_params* params, spx_max_value* d_out,
                          uint32_t* d_counts);
+
+/* ---- batches of uneven beams ---------------------------------------------
+ * No reference counterpart (DspSpectrum transforms one nFFT per call).  A
+ * batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->
+ * spx_next_smooth23(n_point)), the window and TOPK peak parameters
+ * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Inputs are
+ * packed: beam i's samples start at sum_{j<i} n_point[j] (complex64); outputs
+ * are [B x K] MaxValue and [B] counts.  Device scratch is owned by the batch.
+ *  spx_batch_run           all beams in ONE FFT launch + one top-K launch
+ *  spx_batch_run_per_size  the same kernels once per distinct nfft (the
+ *                          per-size baseline; bit-identical results)
+ *  spx_batch_capture/replay  record spx_batch_run for fixed pointers as a
+ *                          CUDA graph on the context's (non-default) stream
+ *  spx_batch_tune/autotune points per thread (16/32) and points per CTA of
+ *                          clustered sizes; autotune times the candidates on
+ *                          the given buffers and keeps the fastest */
+typedef struct spx_batch spx_batch;
+spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_points,
+                            const uint32_t* nffts, uint32_t window,
+                            const spx_peak_params* params, spx_batch** out);
+spx_status spx_batch_destroy(spx_batch* batch);
+uint64_t spx_batch_input_samples(const spx_batch* batch);
+spx_status spx_batch_run(spx_ctx* ctx, spx_batch* batch, const void* d_in,
+                         spx_max_value* d_out, uint32_t* d_counts);
+spx_status spx_batch_run_per_size(spx_ctx* ctx, spx_batch* batch, const void* d_in,
+                                  spx_max_value* d_out, uint32_t* d_counts);
+spx_status spx_batch_capture(spx_ctx* ctx, spx_batch* batch, const void* d_in,
+                             spx_max_value* d_out, uint32_t* d_counts);
+spx_status spx_batch_replay(spx_ctx* ctx, spx_batch* batch);
+spx_status spx_batch_tune(spx_ctx* ctx, spx_batch* batch, uint32_t points_per_thread,
+                          uint32_t points_per_cta);
+spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,
+                              spx_max_value* d_out, uint32_t* d_counts,
+                              uint32_t* best_points_per_thread, uint32_t* best_points_per_cta);
 
 #ifdef __cplusplus
 }  /* extern "C" */

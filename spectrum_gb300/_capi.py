@@ -87,6 +87,15 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_topk": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_fft_peaks": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_all_maxima_noalloc": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
+    "spx_batch_create": (_i, [_vp, _u32, _vp, _vp, _u32, C.POINTER(SpxPeakParams), C.POINTER(_vp)]),
+    "spx_batch_destroy": (_i, [_vp]),
+    "spx_batch_input_samples": (_u64, [_vp]),
+    "spx_batch_run": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "spx_batch_run_per_size": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "spx_batch_capture": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "spx_batch_replay": (_i, [_vp, _vp]),
+    "spx_batch_tune": (_i, [_vp, _vp, _u32, _u32]),
+    "spx_batch_autotune": (_i, [_vp, _vp, _vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32)]),
 }
 
 

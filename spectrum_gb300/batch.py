@@ -1,0 +1,94 @@
+"""Batches of beams with uneven lengths and FFT sizes (spx_batch_* of include/spx.h).
+
+    b = Batch(n_points, window=WINDOW_HANN, k=8, sample_rate=fs)
+    out, counts = b.run(x_packed)            # one FFT launch + one top-K launch
+    out, counts = b.run_per_size(x_packed)   # one launch pair per distinct nfft
+    b.capture(x_packed); b.replay()          # CUDA graph of run() for fixed buffers
+    b.autotune(x_packed)                     # pick points/thread and points/CTA
+
+x_packed holds the beams back to back (complex64, sum(n_points) samples).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import PEAK_TOPK, REFINE_PARABOLIC, WINDOW_NONE, lib
+
+
+class Batch:
+    def __init__(self, n_points, nffts=None, window: int = WINDOW_NONE, k: int = 8,
+                 sample_rate: float = 1.0, refine: int = REFINE_PARABOLIC, search_start: int = 0,
+                 search_end: int = 0, ctx=None):
+        import torch
+
+        from . import default_context
+        self.ctx = ctx or default_context()
+        self.n_points = np.ascontiguousarray(n_points, dtype=np.uint32)
+        self.beams = len(self.n_points)
+        self.k = int(k)
+        nf = None if nffts is None else np.ascontiguousarray(nffts, dtype=np.uint32)
+        p = _capi.peak_params(PEAK_TOPK, search_start, search_end, 0, k, refine, sample_rate, 0.0)
+        h = C.c_void_p()
+        self.ctx.bind_stream()
+        self.ctx.check(lib.spx_batch_create(self.ctx.h, self.beams,
+                                            self.n_points.ctypes.data_as(C.c_void_p),
+                                            nf.ctypes.data_as(C.c_void_p) if nf is not None else None,
+                                            window, C.byref(p), C.byref(h)))
+        self.h = h
+        dev = torch.device("cuda", self.ctx.device)
+        self.out = torch.zeros((self.beams, self.k, 8), dtype=torch.int32, device=dev)
+        self.counts = torch.zeros(self.beams, dtype=torch.int32, device=dev)
+
+    @property
+    def input_samples(self) -> int:
+        return int(lib.spx_batch_input_samples(self.h))
+
+    def _args(self, x):
+        import torch
+        if not (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.complex64 and x.is_contiguous()):
+            raise ValueError("x must be a contiguous CUDA complex64 tensor")
+        if x.numel() != self.input_samples:
+            raise ValueError(f"x holds {x.numel()} samples, the batch needs {self.input_samples}")
+        return (C.c_void_p(x.data_ptr()), C.c_void_p(self.out.data_ptr()), C.c_void_p(self.counts.data_ptr()))
+
+    def run(self, x):
+        self.ctx.bind_stream()
+        self.ctx.check(lib.spx_batch_run(self.ctx.h, self.h, *self._args(x)))
+        return self.out, self.counts
+
+    def run_per_size(self, x):
+        self.ctx.bind_stream()
+        self.ctx.check(lib.spx_batch_run_per_size(self.ctx.h, self.h, *self._args(x)))
+        return self.out, self.counts
+
+    def capture(self, x, stream=None):
+        self.ctx.bind_stream(stream)
+        self.ctx.check(lib.spx_batch_capture(self.ctx.h, self.h, *self._args(x)))
+
+    def replay(self, stream=None):
+        self.ctx.bind_stream(stream)
+        self.ctx.check(lib.spx_batch_replay(self.ctx.h, self.h))
+        return self.out, self.counts
+
+    def tune(self, points_per_thread: int, points_per_cta: int = 0):
+        self.ctx.check(lib.spx_batch_tune(self.ctx.h, self.h, points_per_thread, points_per_cta))
+
+    def autotune(self, x):
+        e, p = C.c_uint32(), C.c_uint32()
+        self.ctx.bind_stream()
+        self.ctx.check(lib.spx_batch_autotune(self.ctx.h, self.h, *self._args(x), C.byref(e), C.byref(p)))
+        return e.value, p.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.spx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -7,7 +7,7 @@ namespace spx {
 
 constexpr int kMaxPass = 12;
 constexpr uint32_t kMaxLocal = 16384;   // points per CTA (one local FFT)
-constexpr uint32_t kPrefLocalCluster = 8192;  // preferred points per CTA when C > 1 (2 CTAs / SM)
+constexpr uint32_t kPrefLocalCluster = 16384;  // preferred points per CTA when C > 1 (measured fastest on GB300)
 constexpr int kEPTDefault = 16;         // points held per thread per pass (16 or 32)
 
 // nfft = C * M.  The M-point local FFT runs npass Stockham passes; pass p

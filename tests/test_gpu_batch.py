@@ -1,0 +1,82 @@
+"""GPU tests of uneven batches (spx_batch_*): the single launch, the per-size
+launches and the CUDA-graph replay give bit-identical top-K lists; without a
+window they also equal the oracle's top-K on spx_fft's spectrum of every beam
+(same FFT code, same plans)."""
+import numpy as np
+import pytest
+
+from oracle import spectrum_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+EXACT = ["index", "real", "imag", "magnitude", "freq_offset", "refined_frequency", "pad"]
+
+
+def _uneven(beams, lo, hi, seed, extra=()):
+    from spectrum_gb300 import synth
+    rng = np.random.default_rng(seed)
+    lengths = list(rng.integers(lo, hi, beams)) + list(extra)
+    bs = synth.make_beams(lengths, tones=(1, 8), snr_db=(0.0, 40.0), seed=seed)
+    rows = synth.synth_numpy(bs)
+    flat = np.concatenate([rows[i, :n] for i, n in enumerate(bs.lengths)])
+    return np.asarray(bs.lengths, np.uint32), flat.astype(np.complex64)
+
+
+def _same(a, b):
+    for f in EXACT + ["phase"]:
+        np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+
+
+@pytest.mark.parametrize("window", [0, 1])
+def test_batch_single_launch_equals_per_size_and_graph(spx, cuda, window):
+    import torch
+    from spectrum_gb300.batch import Batch
+    # sizes cover cluster sizes 1, 2, 3, 4, 6, 8 and 9 (59049 = 3^10)
+    n_points, x = _uneven(40, 1000, 20000, 5, extra=(33000, 52000, 59049, 70000, 99000, 100000))
+    xd = torch.from_numpy(x).to(cuda)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        b = Batch(n_points, window=window, k=8, sample_rate=1.0)
+        o1, c1 = [t.clone() for t in b.run(xd)]
+        o2, c2 = [t.clone() for t in b.run_per_size(xd)]
+        b.capture(xd, stream=s)
+        o3, c3 = [t.clone() for t in b.replay(stream=s)]
+    torch.cuda.synchronize()
+    for o, c in ((o2, c2), (o3, c3)):
+        np.testing.assert_array_equal(c.cpu().numpy(), c1.cpu().numpy())
+        _same(spx.maxvalues_to_numpy(o), spx.maxvalues_to_numpy(o1))
+    assert (c1.cpu().numpy() == 8).all()
+
+
+def test_batch_matches_oracle_without_window(spx, cuda):
+    import torch
+    from spectrum_gb300.batch import Batch
+    n_points, x = _uneven(12, 1000, 30000, 9, extra=(65536, 98000))
+    xd = torch.from_numpy(x).to(cuda)
+    b = Batch(n_points, window=0, k=8, sample_rate=2.0)
+    out, counts = b.run(xd)
+    got = spx.maxvalues_to_numpy(out)
+    counts = counts.cpu().numpy()
+    off = 0
+    for i, n in enumerate(n_points):
+        nfft = spx.next_smooth23(int(n))
+        spec = spx.fft(xd[off:off + n].reshape(1, -1), nfft).cpu().numpy()
+        ref, rc = orc.topk(None, spec, nfft, 2.0, 8)
+        assert counts[i] == rc[0]
+        for f in EXACT:
+            np.testing.assert_array_equal(got[i, : rc[0]][f], ref[0, : rc[0]][f], err_msg=f"beam {i} {f}")
+        off += int(n)
+
+
+def test_batch_autotune_keeps_results(spx, cuda):
+    import torch
+    from spectrum_gb300.batch import Batch
+    n_points, x = _uneven(16, 1000, 40000, 13, extra=(80000,))
+    xd = torch.from_numpy(x).to(cuda)
+    b = Batch(n_points, window=1, k=4)
+    o1, c1 = [t.clone() for t in b.run(xd)]
+    ept, ppc = b.autotune(xd)
+    assert ept in (16, 32) and ppc in (8192, 16384)
+    o2, c2 = b.run(xd)
+    np.testing.assert_array_equal(c1.cpu().numpy(), c2.cpu().numpy())
+    np.testing.assert_array_equal(spx.maxvalues_to_numpy(o1)["index"], spx.maxvalues_to_numpy(o2)["index"])
