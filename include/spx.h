@@ -149,7 +149,8 @@ int spx_abi_version(void);
 uint32_t spx_next_pow2(uint32_t n);
 /* Smallest 2^a*3^b >= n (extension for beams of uneven length). */
 uint32_t spx_next_smooth23(uint32_t n);
-/* 1 if this build can transform nfft points (2^a*3^b, 2 <= nfft <= 2^20), else 0. */
+/* 1 if this build can transform nfft points: 2^a*3^b in [2, 262144] in one
+ * pass (cluster of <= 16 CTAs), or 2^19 / 2^20 in two launches; else 0. */
 int spx_fft_size_supported(uint32_t nfft);
 /* Tuning for transforms of nfft points: points each thread holds per pass
  * (16: more resident warps; 32: more work per thread) and, above 16384

@@ -1,0 +1,146 @@
+// fft_big.cu — transforms of 2^19 and 2^20 points (the precision workload's
+// 2^20-point beams), beyond what one cluster holds on chip.
+//
+// nfft = Cb * M with M = 16384 and Cb in {32, 64}; n = M*n1 + n2, k = k1 + Cb*k2:
+//   launch 1 (big_cols_kernel): for each n2, the Cb-point DFT over n1 of the
+//     windowed, zero-padded samples, times W_N^{n2 k1}, written to
+//     scratch[beam][k1][n2] (device memory);
+//   launch 2 (big_rows_kernel): for each (beam, k1), the M-point Stockham FFT
+//     of row k1 (the passes of fft_core.cuh), X[k1 + Cb*k2] to the output.
+// All twiddles are FP64-generated and stored in FP32 (W_N^m from one table of
+// nfft entries, W_M from the local plan), which is what the 120 dB dynamic
+// range of the precision workload needs.  Replaces hipFFT's internal
+// multi-pass plan for large sizes (src/fft_func/src/fft_processor_rocm.cpp:176-193).
+#include <cmath>
+#include <vector>
+
+#include "fft_core.cuh"
+#include "spx_internal.h"
+
+namespace spx {
+
+constexpr uint32_t kBigM = 16384;
+
+// One tile = 32 consecutive n2 columns x Cb rows (n1), 8 threads per column.
+template <int CB>
+__global__ void __launch_bounds__(256)
+big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+                const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch) {
+  __shared__ float2 tile[CB][33];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t beam = blockIdx.y, n2_0 = blockIdx.x * 32;
+  const float2* x = in + (size_t)beam * n_point;
+  for (uint32_t e = tid; e < CB * 32; e += 256) {
+    const uint32_t n1 = e >> 5, col = e & 31;
+    tile[n1][col] = load_sample(x, n1 * kBigM + n2_0 + col, n_point, win);
+  }
+  __syncthreads();
+  const uint32_t col = tid >> 3, t = tid & 7;
+  constexpr int J = CB / 8;  // stage-1 radix (8 or 4)
+  // stage 1: thread t transforms rows t + 8j (j < J), twiddles W_CB^{t a}
+  float2 v[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) v[j] = tile[t + 8 * j][col];
+  Dft<J>::run(v);
+#pragma unroll
+  for (int a = 1; a < J; ++a) {
+    const uint32_t e = (t * a) % CB;
+    v[a] = cmul(v[a], __ldg(twN + (uint64_t)e * (nfft / CB)));  // W_CB^{e} = W_N^{e N/CB}
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < J; ++a) tile[t + 8 * a][col] = v[a];
+  __syncthreads();
+  // stage 2: for a = t (< J), the 8-point DFT over t' of rows t' + 8a -> k1 = a + J*b
+  if (t < (uint32_t)J) {
+    float2 w[8];
+#pragma unroll
+    for (int tp = 0; tp < 8; ++tp) w[tp] = tile[tp + 8 * t][col];
+    Dft<8>::run(w);
+    const uint32_t n2 = n2_0 + col;
+    float2* o = scratch + (size_t)beam * nfft + n2;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint32_t k1 = t + J * b;
+      const uint64_t m = ((uint64_t)n2 * k1) % nfft;
+      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + m));
+    }
+  }
+}
+
+template <int EPT>
+__global__ void __launch_bounds__(kMaxLocal / EPT, 1)
+big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ scratch,
+                void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  const uint32_t tid = threadIdx.x, T = blockDim.x;
+  const uint32_t beam = blockIdx.x / g.C, k1 = blockIdx.x % g.C;
+  const float2* row = scratch + (size_t)beam * g.nfft + (size_t)k1 * g.M;
+  first_pass_dispatch<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tid, T);
+  local_passes<EPT>(s, g, 1, tw_local, tid, T);
+  epilogue_out(s, g, k1, beam, out, out_mode, scale, tid, T);
+}
+
+bool big_size(uint32_t nfft) { return nfft == (1u << 19) || nfft == (1u << 20); }
+
+// Geometry of the row FFTs (M = 16384, C = Cb as the output stride) and the
+// W_N table; called by get_plan for big sizes.
+spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
+  FftGeom gl{};
+  if (!build_geom(kBigM, &gl, kEPTDefault)) return fail(ctx, SPX_ERR_INVALID_ARG, "big plan");
+  gl.nfft = nfft;
+  gl.C = nfft / kBigM;
+  plan->g = gl;
+  plan->big = true;
+  std::vector<float2> twl(kBigM);
+  for (uint32_t p = 0; p < gl.npass; ++p) {
+    const uint32_t R = gl.radix[p], Ns = gl.ns[p];
+    for (uint32_t r = 1; r < R; ++r)
+      for (uint32_t k = 0; k < Ns; ++k) {
+        const uint64_t L = (uint64_t)Ns * R, m = ((uint64_t)r * k) % L;
+        const double a = -2.0 * M_PI * (double)m / (double)L;
+        twl[gl.twoff[p] + (r - 1) * Ns + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
+  }
+  std::vector<float2> twn(nfft);
+  for (uint32_t m = 0; m < nfft; ++m) {
+    const double a = -2.0 * M_PI * (double)m / (double)nfft;
+    twn[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&plan->d_tw_cross, twn.size() * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(plan->d_tw_cross, twn.data(), twn.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "big plan tables");
+  return SPX_OK;
+}
+
+spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
+                          uint32_t n_point, const float* d_win, uint32_t out_mode, float scale,
+                          void* d_out) {
+  if (beams == 0) return SPX_OK;
+  const FftGeom& g = plan.g;
+  void* scr = nullptr;
+  spx_status st = get_scratch(ctx, kSlotExchange, (size_t)beams * g.nfft * sizeof(float2), &scr);
+  if (st != SPX_OK) return st;
+  float2* scratch = static_cast<float2*>(scr);
+  dim3 grid(kBigM / 32, beams);
+  if (g.C == 64)
+    big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch);
+  else
+    big_cols_kernel<32><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
+  const void* kfn = (const void*)big_rows_kernel<kEPTDefault>;
+  e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows_kernel");
+  FftGeom gg = g;
+  const float2* twl = plan.d_tw_local;
+  const float2* sc = scratch;
+  void* args[] = {(void*)&gg, (void*)&twl, (void*)&sc, (void*)&d_out, (void*)&out_mode, (void*)&scale};
+  e = cudaLaunchKernel(kfn, dim3(beams * g.C), dim3(g.T), args, (size_t)g.Mpad * sizeof(float2), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_rows_kernel");
+  return SPX_OK;
+}
+
+}  // namespace spx

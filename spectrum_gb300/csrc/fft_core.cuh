@@ -25,6 +25,7 @@
 
 #include <cooperative_groups.h>
 
+#include "spx.h"
 #include "spx_device.cuh"
 #include "spx_geom.h"
 
@@ -198,6 +199,38 @@ SPX_DEV void local_passes(float2* s, const FftGeom& g, uint32_t p0,
   p = run_radix<3, EPT>(s, g, p, tw_local, tid, T);
   p = run_radix<4, EPT>(s, g, p, tw_local, tid, T);
   p = run_radix<2, EPT>(s, g, p, tw_local, tid, T);
+}
+
+// Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
+SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
+                          void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
+                          uint32_t T) {
+  const size_t obase = (size_t)beam * g.nfft + c;
+  switch (out_mode) {
+    case SPX_OUT_COMPLEX: {
+      float2* o = reinterpret_cast<float2*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = s[sw(i)];
+      break;
+    }
+    case SPX_OUT_MAG: {
+      float* o = reinterpret_cast<float*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag_rn(s[sw(i)]), scale);
+      break;
+    }
+    case SPX_OUT_MAG2: {
+      float* o = reinterpret_cast<float*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag2_rn(s[sw(i)]), scale);
+      break;
+    }
+    default: {  // SPX_OUT_MAGPHASE
+      float2* o = reinterpret_cast<float2*>(out) + obase;
+      for (uint32_t i = tid; i < g.M; i += T) {
+        float2 z = s[sw(i)];
+        o[(size_t)g.C * i] = make_float2(mag_rn(z), atan2f(z.y, z.x));
+      }
+      break;
+    }
+  }
 }
 
 }  // namespace spx

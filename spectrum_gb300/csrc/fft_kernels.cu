@@ -20,40 +20,6 @@
 namespace spx {
 
 // ---------------------------------------------------------------------------
-// Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
-// ---------------------------------------------------------------------------
-SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
-                          void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
-                          uint32_t T) {
-  const size_t obase = (size_t)beam * g.nfft + c;
-  switch (out_mode) {
-    case SPX_OUT_COMPLEX: {
-      float2* o = reinterpret_cast<float2*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = s[sw(i)];
-      break;
-    }
-    case SPX_OUT_MAG: {
-      float* o = reinterpret_cast<float*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag_rn(s[sw(i)]), scale);
-      break;
-    }
-    case SPX_OUT_MAG2: {
-      float* o = reinterpret_cast<float*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag2_rn(s[sw(i)]), scale);
-      break;
-    }
-    default: {  // SPX_OUT_MAGPHASE
-      float2* o = reinterpret_cast<float2*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) {
-        float2 z = s[sw(i)];
-        o[(size_t)g.C * i] = make_float2(mag_rn(z), atan2f(z.y, z.x));
-      }
-      break;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Kernel for nfft <= 16384: one CTA per beam.
 // ---------------------------------------------------------------------------
 template <int EPT>
@@ -192,9 +158,16 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
     return SPX_OK;
   }
   auto plan = std::make_unique<FftPlan>();
+  if (big_size(nfft)) {
+    spx_status st = build_big_plan(ctx, nfft, plan.get());
+    if (st != SPX_OK) return st;
+    *out = plan.get();
+    ctx->plans.emplace(key, std::move(plan));
+    return SPX_OK;
+  }
   if (!build_geom(nfft, &plan->g, ept, pref))
     return fail(ctx, SPX_ERR_INVALID_ARG,
-                "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b, 2..262144)");
+                "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b up to 262144, or 2^19, 2^20)");
   const FftGeom& g = plan->g;
   std::vector<float2> twl(std::max<uint32_t>(g.M, 1));
   for (uint32_t p = 0; p < g.npass; ++p) {
@@ -313,6 +286,7 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
                           uint32_t beams, uint32_t n_point, const float* d_win,
                           uint32_t out_mode, float scale, void* d_out) {
   if (beams == 0) return SPX_OK;
+  if (plan.big) return launch_fft_big(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
   FftGeom g = plan.g;
   const float2* twl = plan.d_tw_local;
   const float2* twc = plan.d_tw_cross;

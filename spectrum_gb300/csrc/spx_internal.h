@@ -18,7 +18,8 @@ namespace spx {
 struct FftPlan {
   FftGeom g{};
   float2* d_tw_local = nullptr;  // M - 1 entries (>= 1 allocated)
-  float2* d_tw_cross = nullptr;  // (C - 1) * M entries, or null when C == 1
+  float2* d_tw_cross = nullptr;  // (C - 1) * M entries (big plans: W_N^m, nfft entries)
+  bool big = false;              // two-launch transform (2^19, 2^20 points)
   ~FftPlan();
 };
 
@@ -72,6 +73,13 @@ spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
 // Raises a kernel's dynamic shared-memory limit (and allows clusters of
 // up to 16) once per (device, kernel).
 cudaError_t configure_kernel(const void* kernel, size_t max_smem);
+
+// Two-launch transforms of 2^19 and 2^20 points (fft_big.cu).
+bool big_size(uint32_t nfft);
+spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
+spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
+                          uint32_t n_point, const float* d_win, uint32_t out_mode, float scale,
+                          void* d_out);
 
 // Fused FFT + peak search (fft_peaks.cu).
 bool fused_supported(const FftGeom& g, uint32_t mode);

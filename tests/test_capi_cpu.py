@@ -52,9 +52,9 @@ def test_next_smooth23_matches_oracle(lib):
 
 
 def test_fft_size_support(lib):
-    for n in (2, 3, 8, 4096, 13122, 59049, 104976, 131072, 262144):
+    for n in (2, 3, 8, 4096, 13122, 59049, 104976, 131072, 262144, 1 << 19, 1 << 20):
         assert lib.spx_fft_size_supported(n) == 1, n
-    for n in (0, 1, 5, 1000, 524289):
+    for n in (0, 1, 5, 1000, 524289, 3 << 18, 1 << 21):
         assert lib.spx_fft_size_supported(n) == 0, n
 
 

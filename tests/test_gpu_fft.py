@@ -22,7 +22,7 @@ FFT_CASES = [
     (4096, 4096, 1), (6561, 6561, 0), (13122, 13000, 2), (13824, 13824, 0), (16384, 16384, 1),
     (17496, 17000, 0), (19683, 19683, 0), (32768, 20000, 1), (52488, 52000, 0),
     (65536, 65536, 3), (69984, 69000, 1), (104976, 100000, 1), (131072, 65536, 1),
-    (59049, 59049, 0), (262144, 262144, 0),
+    (59049, 59049, 0), (262144, 262144, 0), (1 << 19, 300000, 1), (1 << 20, 1 << 20, 4),
 ]
 
 
@@ -40,7 +40,7 @@ def _max_rel(a, b):
 @pytest.mark.parametrize("nfft,n_point,win", FFT_CASES)
 def test_fft_complex_matches_pocketfft(spx, cuda, nfft, n_point, win):
     import torch
-    beams = 3 if nfft <= 65536 else 2
+    beams = 3 if nfft <= 65536 else (2 if nfft <= 262144 else 1)
     x = _signal(beams, n_point, nfft + n_point)
     got = spx.fft(torch.from_numpy(x).to(cuda), nfft, window=win).cpu().numpy()
     ref32 = orc.fft_fp32(x, nfft, win)
@@ -98,4 +98,26 @@ def test_fft_rejects_bad_sizes(spx, cuda):
     with pytest.raises(ValueError):
         spx.fft(x, 1000)         # 1000 = 2^3 * 5^3 is not 2^a 3^b
     with pytest.raises(ValueError):
-        spx.fft(x, 1 << 20)      # beyond the single-pass limit
+        spx.fft(x, 3 << 18)      # 2^18 * 3 exceeds the single-pass limit and is no two-launch size
+
+
+def test_precision_workload_dynamic_range(spx, cuda):
+    """Two tones 120 dB apart + noise 1e-7, Blackman-Harris, 2^20 points: the
+    FP32 transform (FP64-generated twiddles) stays within 1e-6 of the FP64
+    spectrum's peak and the weak tone stands far above the error floor."""
+    import torch
+    from spectrum_gb300 import synth
+    bs = synth.workload_precision(seed=3, beams=2)
+    x = synth.synth_numpy(bs)
+    n = 1 << 20
+    got = spx.fft(torch.from_numpy(x).to(cuda), n, window=spx.WINDOW_BLACKMAN_HARRIS).cpu().numpy()
+    ref = orc.fft_fp64(x, n, orc.WINDOW_BLACKMAN_HARRIS)
+    for b in range(2):
+        peak = np.abs(ref[b]).max()
+        err = np.abs(got[b] - ref[b])
+        assert err.max() / peak < 1e-6, err.max() / peak
+        rms = np.sqrt(np.mean(err ** 2))
+        weak = int(round(bs.freqs[b][1] * n))
+        weak_mag = np.abs(got[b, weak - 2:weak + 3]).max()
+        assert 20 * np.log10(peak / rms) > 150          # dynamic range vs the FP32 error floor
+        assert 20 * np.log10(weak_mag / rms) > 40       # the -120 dB tone is visible
