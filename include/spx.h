@@ -113,7 +113,7 @@ enum spx_peak_mode {
  *    bins [0, range/2) and [nfft-range/2, nfft) are searched.
  *  max_per_beam: ALL: output capacity per beam is
  *    min((end-start)/2, max_per_beam) (all_maxima_pipeline_rocm.cpp:304-307);
- *    TOPK: K (1..64).
+ *    TOPK: K (1..32).
  *  thresh_sigma: ALL/TOPK: keep maxima with |X| > noise_median * f(thresh_sigma)
  *    (see spx_noise_threshold_factor); 0 disables the threshold (reference
  *    behaviour).
@@ -275,6 +275,62 @@ spx_status spx_batch_tune(spx_ctx* ctx, spx_batch* batch, uint32_t points_per_th
 spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,
                               spx_max_value* d_out, uint32_t* d_counts,
                               uint32_t* best_points_per_thread, uint32_t* best_points_per_cta);
+
+/* ---- learned sub-bin refinement ------------------------------------------
+ * No reference counterpart: it stands beside the 3-point parabola of
+ * include/spectrum/kernels/fft_kernel_sources_rocm.hpp:228-239 (the parabola
+ * stays the fallback).  A 10 -> 64 -> 64 -> 2 GELU network with BF16 weights
+ * and FP32 accumulation maps the 5 bins around a peak (|X[k+d]|/|X[k]| and
+ * the window-corrected phase of X[k+d] conj X[k], d = -2..2) to the tone's
+ * offset from bin k (bins) and log(amplitude / |X[k]|).
+ * Parameters: spx_mlp_param_count() floats, layout W1[64][10] b1[64]
+ * W2[64][64] b2[64] W3[2][64] b3[2] (FP32 masters; products read the BF16
+ * rounding of the weights; biases are FP32).
+ *  spx_mlp_make_frames  single-tone Hann frames made on the GPU: per frame the
+ *                       features [10], the target [2] from a 16x zero-padded
+ *                       FFT of the same frame, the parabolic result [2] =
+ *                       (bin k, parabola offset), valid [1] and optionally
+ *                       the truth [2] = (frequency in cycles/sample, SNR dB)
+ *  spx_mlp_forward      Y[rows][2] from X[rows][10]
+ *  spx_mlp_gradients    gradient of the masked mean squared error (mask NULL
+ *                       = every row) w.r.t. the parameters; *d_loss += loss
+ *  spx_mlp_train_step   one Adam step (beta 0.9 / 0.999, eps 1e-8)
+ *  spx_mlp_train        epochs over rows (a power of two) in minibatches,
+ *                       cosine learning rate lr_max -> lr_min, per-epoch mean
+ *                       loss into d_epoch_loss[epochs] (may be NULL)
+ *  spx_mlp_refine       rewrites freq_offset / refined_frequency of the
+ *                       [beams x K] peaks of a TOPK/ALL search with counts;
+ *                       keeps the parabolic values when the network's offset
+ *                       leaves the bin; d_amplitude [beams x K] (may be NULL)
+ *                       receives |X[k]| exp(y1); d_used_mlp (may be NULL)
+ *                       1 where the network was used.
+ * Training-data generation and training allocate; forward/refine allocate
+ * activations only when a larger row count is first seen. */
+typedef struct spx_mlp spx_mlp;
+uint32_t spx_mlp_param_count(void);
+spx_status spx_mlp_create(spx_ctx* ctx, uint64_t seed, spx_mlp** out);
+spx_status spx_mlp_destroy(spx_mlp* mlp);
+spx_status spx_mlp_set_params(spx_ctx* ctx, spx_mlp* mlp, const float* host_params);
+spx_status spx_mlp_get_params(spx_ctx* ctx, spx_mlp* mlp, float* host_params);
+spx_status spx_mlp_make_frames(spx_ctx* ctx, uint64_t seed, uint32_t frame0, uint32_t frames,
+                               uint32_t nfft, float snr_lo_db, float snr_hi_db, float* d_feat,
+                               float* d_target, float* d_parabolic, uint32_t* d_valid,
+                               float* d_truth);
+spx_status spx_mlp_forward(spx_ctx* ctx, spx_mlp* mlp, const float* d_x, uint32_t rows,
+                           float* d_y);
+spx_status spx_mlp_gradients(spx_ctx* ctx, spx_mlp* mlp, const float* d_x, const float* d_t,
+                             const uint32_t* d_mask, uint32_t rows, float* d_grad,
+                             float* d_loss);
+spx_status spx_mlp_train_step(spx_ctx* ctx, spx_mlp* mlp, const float* d_x, const float* d_t,
+                              const uint32_t* d_mask, uint32_t rows, float lr, float* d_loss);
+spx_status spx_mlp_train(spx_ctx* ctx, spx_mlp* mlp, const float* d_feat,
+                         const float* d_target, const uint32_t* d_valid, uint32_t rows,
+                         uint32_t batch, uint32_t epochs, float lr_max, float lr_min,
+                         uint64_t seed, float* d_epoch_loss);
+spx_status spx_mlp_refine(spx_ctx* ctx, spx_mlp* mlp, const void* d_fft, uint32_t beams,
+                          uint32_t n_point, uint32_t nfft, float sample_rate, uint32_t K,
+                          spx_max_value* d_peaks, const uint32_t* d_counts,
+                          float* d_amplitude, uint32_t* d_used_mlp);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -96,6 +96,17 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_batch_replay": (_i, [_vp, _vp]),
     "spx_batch_tune": (_i, [_vp, _vp, _u32, _u32]),
     "spx_batch_autotune": (_i, [_vp, _vp, _vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32)]),
+    "spx_mlp_param_count": (_u32, []),
+    "spx_mlp_create": (_i, [_vp, _u64, C.POINTER(_vp)]),
+    "spx_mlp_destroy": (_i, [_vp]),
+    "spx_mlp_set_params": (_i, [_vp, _vp, _vp]),
+    "spx_mlp_get_params": (_i, [_vp, _vp, _vp]),
+    "spx_mlp_make_frames": (_i, [_vp, _u64, _u32, _u32, _u32, _f, _f, _vp, _vp, _vp, _vp, _vp]),
+    "spx_mlp_forward": (_i, [_vp, _vp, _vp, _u32, _vp]),
+    "spx_mlp_gradients": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _vp, _vp]),
+    "spx_mlp_train_step": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _f, _vp]),
+    "spx_mlp_train": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f, _f, _u64, _vp]),
+    "spx_mlp_refine": (_i, [_vp, _vp, _vp, _u32, _u32, _u32, _f, _u32, _vp, _vp, _vp, _vp]),
 }
 
 

@@ -43,20 +43,6 @@ spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out) {
   return SPX_OK;
 }
 
-// Makes ctx's device current for the duration of an entry point.
-struct DeviceGuard {
-  int prev = -1;
-  bool ok = true;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
-
 // Resolves ALL / TOPK window defaults (spectrum_processor_rocm.cpp:703-705).
 static void resolve_window(uint32_t nfft, uint32_t* start, uint32_t* end) {
   if (*start == 0) *start = 1;

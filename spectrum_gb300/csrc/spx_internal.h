@@ -123,4 +123,18 @@ spx_status launch_noise_threshold(spx_ctx* ctx, const float* d_mag, const float2
                                   uint32_t beams, uint32_t nfft, uint32_t start,
                                   uint32_t end, float factor, float* d_thr);
 
+// Makes ctx's device current for the duration of an entry point.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
 }  // namespace spx

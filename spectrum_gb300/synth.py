@@ -93,6 +93,11 @@ def workload_precision(seed: int = 3, beams: int = 64, n: int = 1 << 20):
     return BeamSet(np.full(beams, n, np.int64), fs, as_, ps, np.full(beams, 1e-7), seed)
 
 
+def workload_learned(seed: int = 4, beams: int = 4096, n: int = 8192, snr_db: float = 20.0) -> BeamSet:
+    """4096 beams x 8192, one tone each at a fixed SNR (learned-refinement inference)."""
+    return make_beams([n] * beams, tones=(1, 1), snr_db=(snr_db, snr_db), seed=seed)
+
+
 # ---- synthesis -----------------------------------------------------------------
 def synth_numpy(bs: BeamSet, pad_to: int | None = None) -> np.ndarray:
     """Rows of length max(lengths) (or pad_to), zero beyond each beam's length."""
