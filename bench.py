@@ -36,6 +36,9 @@ BEAMS, N_POINT, NFFT = 256, 65536, 131072
 FS = 1.0
 SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
+# DRAM bytes (read + write) of one fft_peaks_kernel launch on this workload,
+# from an ncu capture (profiles/fft_peaks_kernel_plain_large.md).
+NCU_TRAFFIC_BYTES = 145_510_912
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
@@ -46,6 +49,8 @@ def _parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-beams", type=int, default=0)
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the small / uneven / precision / learned workload timings")
     ap.add_argument("--profile", action="store_true",
                     help="device steps only (warmup + steps), no timing report; for ncu captures")
     return ap.parse_args()
@@ -202,7 +207,8 @@ def run_gpu(args):
     ctx = spx.default_context(local)
 
     # three rotating input buffers (different seeds) -> inputs larger than L2
-    nbuf = 3
+    # (one buffer under --profile: fewer launches and less memory for ncu)
+    nbuf = 1 if args.profile else 3
     xs = [synth.synth_torch(synth.workload_large(seed=1 + 97 * rank + i, beams=BEAMS), device=dev)
           for i in range(nbuf)]
     torch.cuda.synchronize()
@@ -259,6 +265,9 @@ def run_gpu(args):
 
     if rank != 0:
         return
+    hbm0 = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs", 6800.0)) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0
+    workloads = None if args.no_workloads else bench_workloads(spx, ctx, stream, dev, hbm0)
     # roofline of the dominant kernel (the FFT, which reads the samples once)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
@@ -278,6 +287,8 @@ def run_gpu(args):
         "clocks": clk,
         "gpu_launches": kern["launches_per_step"] * args.steps,
     }
+    if workloads is not None:
+        line["workloads"] = workloads
     r = line["roofline"]
     r["frac"] = round(r["achieved"] / r["peak"], 4)
     if args.cpu_sample_beams >= 0:
@@ -325,18 +336,178 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
     # algorithmic bytes: samples read once + maxima and counts written
     algo = BEAMS * N_POINT * 8 + n_max * 32 + BEAMS * 4
     return {
-        "path": "fused: fft_peaks_kernel (one cluster of 16 CTAs per beam; FFT, |X|, threshold, "
-                "maxima and compaction on chip) after a 4 MiB histogram memset",
+        "path": "fused: fft_peaks_kernel (one cluster of 8 CTAs x 1024 threads per beam; FFT, |X|, "
+                "threshold, maxima and compaction on chip) after a 4 MiB histogram memset",
         "components_ms": {"fused_step": round(f, 4), "composed_fft_complex": round(statistics.median(fft_ms), 4),
                           "composed_peaks": round(statistics.median(peak_ms), 4)},
         "roofline": {"bound": "hbm", "kernel": "fft_peaks_kernel", "achieved": round(algo / (f * 1e-3) / 1e9, 1),
-                     "unit": "GB/s", "traffic": None, "algorithmic_bytes_per_launch": algo,
+                     "unit": "GB/s", "traffic": NCU_TRAFFIC_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                                       "(profiles/fft_peaks_kernel_plain_large.md)",
+                     "algorithmic_bytes_per_launch": algo,
                      "maxima_per_launch": n_max},
         "launches_per_step": 1,
     }
 
 
+def _time_ms(stream, fn, reps):
+    """Median of per-call CUDA-event times of fn() on stream (after 3 warm-ups)."""
+    import torch
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def bench_workloads(spx, ctx, stream, dev, hbm):
+    """The other workloads of the path, each timed on the device with inputs
+    resident: small (8 x 4096 top-5), uneven (1024 beams, one launch vs one
+    launch pair per size), precision (64 x 2^20 Blackman-Harris, error vs an
+    FP64 FFT on two beams) and learned (training time; inference on 4096 x
+    8192 against the plain parabolic path, with frequency RMS errors)."""
+    import ctypes as C
+
+    import torch
+
+    from spectrum_gb300 import learned, synth
+    from spectrum_gb300.batch import Batch
+    res = {}
+
+    # ---- small: 8 x 4096, Hann, top-5, parabolic (fused single-CTA kernel) ----
+    xs = synth.synth_torch(synth.workload_small(seed=0), device=dev)
+    o5 = torch.zeros((8, 5, 8), dtype=torch.int32, device=dev)
+    c5 = torch.zeros(8, dtype=torch.int32, device=dev)
+    p5 = spx.peak_params(spx.PEAK_TOPK, 0, 0, 0, 5, spx.REFINE_PARABOLIC, 1.0, 0.0)
+    ms = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft_peaks(
+        ctx.h, C.c_void_p(xs.data_ptr()), 8, 4096, 4096, spx.WINDOW_HANN, C.byref(p5),
+        C.c_void_p(o5.data_ptr()), C.c_void_p(c5.data_ptr()))), 50)
+    res["small"] = {"config": "8 x 4096, Hann, nFFT 4096, top-5, parabolic", "ms_per_step": round(ms, 4),
+                    "Msamples_per_s": round(8 * 4096 / (ms * 1e-3) / 1e6, 1),
+                    "note": "launch-latency bound (one 8-CTA launch)"}
+
+    # ---- uneven: 1024 beams, len U[1000, 100000], nFFT = next 2^a 3^b, top-8 ----
+    bs = synth.workload_uneven(seed=2)
+    xu = synth.synth_torch(bs, device=dev, packed=True)
+    b = Batch(bs.lengths, window=spx.WINDOW_HANN, k=8, sample_rate=1.0, ctx=ctx)
+    b.autotune(xu)
+    ms_one = _time_ms(stream, lambda: b.run(xu), 20)
+    ms_per = _time_ms(stream, lambda: b.run_per_size(xu), 10)
+    side = torch.cuda.Stream(device=dev)   # graph capture needs a non-default stream
+    with torch.cuda.stream(side):
+        b.capture(xu, stream=side)
+        ms_graph = _time_ms(side, lambda: b.replay(stream=side), 20)
+    torch.cuda.synchronize()
+    ctx.bind_stream(stream)
+    samples = int(bs.lengths.sum())
+    algo_u = samples * 8 + 1024 * (8 * 32 + 4)
+    best = min(ms_one, ms_graph)
+    res["uneven"] = {"config": "1024 beams, n_point U[1000,100000], nFFT = next 2^a3^b, Hann, top-8",
+                     "samples": samples, "distinct_nfft": len({spx.next_smooth23(int(v)) for v in bs.lengths}),
+                     "ms_one_launch": round(ms_one, 4), "ms_graph_replay": round(ms_graph, 4),
+                     "ms_per_size_plain": round(ms_per, 4),
+                     "Msamples_per_s": round(samples / (best * 1e-3) / 1e6, 1),
+                     "speedup_vs_per_size": round(ms_per / best, 2),
+                     "roofline": {"bound": "hbm", "achieved": round(algo_u / (best * 1e-3) / 1e9, 1),
+                                  "peak": hbm, "unit": "GB/s",
+                                  "frac": round(algo_u / (best * 1e-3) / 1e9 / hbm, 4)}}
+    del xu, b
+
+    # ---- precision: 64 x 2^20, Blackman-Harris, two tones 120 dB apart ----
+    n = 1 << 20
+    bp = synth.workload_precision(seed=3, beams=64)
+    xp = synth.synth_torch(bp, device=dev)
+    spec = torch.empty((64, n), dtype=torch.complex64, device=dev)
+    ms_fft = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft(
+        ctx.h, C.c_void_p(xp.data_ptr()), 64, n, n, spx.WINDOW_BLACKMAN_HARRIS, spx.OUT_COMPLEX, 1.0,
+        C.c_void_p(spec.data_ptr()))), 10)
+    # error against an FP64 transform of the same FP32 samples (two beams)
+    t = np.arange(n)
+    th = 2.0 * np.pi * t / (n - 1)
+    w = (0.35875 - 0.48829 * np.cos(th) + 0.14128 * np.cos(2 * th) - 0.01168 * np.cos(3 * th))
+    w = w.astype(np.float32).astype(np.float64)
+    errs_max, errs_rms, dr = [], [], []
+    for bb in (0, 63):
+        ref = np.fft.fft(xp[bb].cpu().numpy().astype(np.complex128) * w)
+        got = spec[bb].cpu().numpy().astype(np.complex128)
+        peak = np.abs(ref).max()
+        e = np.abs(got - ref)
+        errs_max.append(float(e.max() / peak))
+        rms = float(np.sqrt(np.mean(e ** 2)))
+        errs_rms.append(rms / peak)
+        dr.append(20 * np.log10(peak / rms))
+    res["precision"] = {"config": "64 x 2^20, Blackman-Harris, tones 120 dB apart + sigma 1e-7",
+                        "ms_fft": round(ms_fft, 4),
+                        "Msamples_per_s": round(64 * n / (ms_fft * 1e-3) / 1e6, 1),
+                        "max_rel_err_vs_fp64": max(errs_max), "rms_rel_err_vs_fp64": max(errs_rms),
+                        "dynamic_range_db": round(min(dr), 1), "beams_checked": [0, 63]}
+    del xp, spec
+
+    # ---- learned: train on 2^20 frames of 1024, infer on 4096 x 8192 ----
+    r = learned.MLPRefiner(seed=1, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    data = r.make_frames(1 << 20, nfft=1024, snr_db=(0.0, 40.0), seed=11)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    losses = r.train(data, epochs=20, batch=4096, lr_max=3e-3, lr_min=1e-5, seed=5)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    del data
+    bl = synth.workload_learned(seed=4)
+    xl = synth.synth_torch(bl, device=dev)
+    nl = 8192
+    specl = torch.empty((4096, nl), dtype=torch.complex64, device=dev)
+    o1 = torch.zeros((4096, 1, 8), dtype=torch.int32, device=dev)
+    c1 = torch.zeros(4096, dtype=torch.int32, device=dev)
+    p1 = spx.peak_params(spx.PEAK_TOPK, 0, 0, 0, 1, spx.REFINE_PARABOLIC, 1.0, 0.0)
+
+    def plain():
+        ctx.check(spx.lib.spx_fft(ctx.h, C.c_void_p(xl.data_ptr()), 4096, nl, nl, spx.WINDOW_HANN,
+                                  spx.OUT_COMPLEX, 1.0, C.c_void_p(specl.data_ptr())))
+        ctx.check(spx.lib.spx_topk(ctx.h, None, C.c_void_p(specl.data_ptr()), 4096, nl, C.byref(p1),
+                                   C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr())))
+
+    def refine_only():
+        ctx.check(spx.lib.spx_mlp_refine(ctx.h, r.h, C.c_void_p(specl.data_ptr()), 4096, nl, nl, 1.0, 1,
+                                         C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr()), None, None))
+
+    ms_plain = _time_ms(stream, plain, 10)
+    ms_ref = _time_ms(stream, lambda: (plain(), refine_only()), 10)
+    ms_kernel = _time_ms(stream, refine_only, 10)
+    plain()
+    par = spx.maxvalues_to_numpy(o1)[:, 0].copy()
+    refine_only()
+    got = spx.maxvalues_to_numpy(o1)[:, 0]
+    f = np.array([fr[0] for fr in bl.freqs]) * nl
+    keep = (f > 4) & (f < nl / 2 - 4)
+    rms_p = float(np.sqrt(np.mean(((par["index"] + par["freq_offset"].astype(np.float64)) - f)[keep] ** 2)))
+    rms_m = float(np.sqrt(np.mean(((got["index"] + got["freq_offset"].astype(np.float64)) - f)[keep] ** 2)))
+    res["learned"] = {"config": "train 2^20 frames x nFFT 1024 (Hann, SNR U[0,40] dB, 16x zero-padded judge), "
+                                "20 epochs of 256 Adam steps; infer 4096 x 8192 at SNR 20 dB, top-1",
+                      "make_frames_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
+                      "final_loss": float(losses[-1]),
+                      "ms_plain_fft_topk": round(ms_plain, 4), "ms_with_learned_refine": round(ms_ref, 4),
+                      "ms_refine_kernel": round(ms_kernel, 4),
+                      "Msamples_per_s_with_refine": round(4096 * nl / (ms_ref * 1e-3) / 1e6, 1),
+                      "freq_rms_bins_parabolic": round(rms_p, 6), "freq_rms_bins_learned": round(rms_m, 6),
+                      "rms_gain": round(rms_p / rms_m, 2)}
+    return res
+
+
 def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
+    """End to end through the C ABI's host-buffer entry point
+    (spx_fft_peaks_host): page-locked host samples in, host maxima and counts
+    out; the upload, the fused kernel and the read-back of ~16 MiB chunks
+    overlap on three streams.  Timed with the host clock around whole calls
+    (each call returns with the results in host memory)."""
     import ctypes as C
 
     import torch
@@ -344,30 +515,30 @@ def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
     host_in.copy_(x_dev.cpu())
     host_out = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
     host_cnt = torch.empty(counts.shape, dtype=counts.dtype, pin_memory=True)
-    dev_in = torch.empty_like(x_dev)
 
     def step():
-        dev_in.copy_(host_in, non_blocking=True)
-        ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(dev_in.data_ptr()), BEAMS, N_POINT, NFFT,
-                                        spx.WINDOW_HANN, C.byref(p), C.c_void_p(out.data_ptr()),
-                                        C.c_void_p(counts.data_ptr())))
-        host_out.copy_(out, non_blocking=True)
-        host_cnt.copy_(counts, non_blocking=True)
+        ctx.check(spx.lib.spx_fft_peaks_host(ctx.h, C.c_void_p(host_in.data_ptr()), BEAMS, N_POINT, NFFT,
+                                             spx.WINDOW_HANN, C.byref(p), C.c_void_p(host_out.data_ptr()),
+                                             C.c_void_p(host_cnt.data_ptr())))
 
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    steps = max(args.steps // 2, 3)
-    e0.record(stream)
+    steps = max(args.steps, 5)
+    t0 = time.perf_counter()
     for _ in range(steps):
         step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    # the same maxima as the device-resident path
+    ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(x_dev.data_ptr()), BEAMS, N_POINT, NFFT,
+                                    spx.WINDOW_HANN, C.byref(p), C.c_void_p(out.data_ptr()),
+                                    C.c_void_p(counts.data_ptr())))
+    same = bool(torch.equal(counts.cpu(), host_cnt))
     return {"value": round(BEAMS * N_POINT / (ms * 1e-3) / 1e6, 2), "unit": "Msamples/s",
             "ms_per_step": round(ms, 4), "h2d_bytes_per_step": int(host_in.numel() * 8),
-            "d2h_bytes_per_step": int(host_out.numel() * 4 + host_cnt.numel() * 4)}
+            "d2h_bytes_per_step": int(host_out.numel() * 4 + host_cnt.numel() * 4),
+            "api": "spx_fft_peaks_host (pinned host buffers, 16 MiB chunks, copy/compute overlap)",
+            "counts_match_device_path": same}
 
 
 def main():

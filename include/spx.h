@@ -242,6 +242,22 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
                          const spx_peak_params* params, spx_max_value* d_out,
                          uint32_t* d_counts);
 
+/* ---- fused, host buffers -------------------------------------------------
+ * spx_fft_peaks from host memory to host memory: the reference's
+ * ISpectrumProcessor::ProcessFromCPU / FindAllMaximaFromCPU with
+ * OutputDestination::CPU (include/spectrum/interface/i_spectrum_processor.hpp:85-86,
+ * 117-119; src/fft_func/src/spectrum_processor_rocm.cpp:444-500).  h_in holds
+ * beams x n_point complex64; h_out receives beams x R MaxValue (R = 4 ONE,
+ * 8 TWO, the spx_all_maxima_capacity for ALL, K for TOPK) and h_counts the
+ * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO).  The beams go through
+ * in ~16 MiB chunks whose upload, transform and read-back overlap on three
+ * streams; page-locked host buffers (cudaHostAlloc / cudaHostRegister) are
+ * needed for the overlap.  Returns after the results are in host memory. */
+spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
+                              uint32_t n_point, uint32_t nfft, uint32_t window,
+                              const spx_peak_params* params, spx_max_value* h_out,
+                              uint32_t* h_counts);
+
 /* ---- batches of uneven beams ---------------------------------------------
  * No reference counterpart (DspSpectrum transforms one nFFT per call).  A
  * batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->

@@ -222,6 +222,42 @@ def fft_peaks(x, nfft: int, window: int = WINDOW_NONE, mode: int = PEAK_ALL,
     return o, counts
 
 
+def fft_peaks_host(x, nfft: int, window: int = WINDOW_NONE, mode: int = PEAK_ALL,
+                   sample_rate: float = 1000.0, search_start: int = 0, search_end: int = 0,
+                   search_range: int = 0, max_per_beam: int = 1000, refine: int = REFINE_NONE,
+                   thresh_sigma: float = 0.0, out=None, counts=None, ctx: Context | None = None):
+    """Host samples [beams, n_point] complex64 (numpy array or CPU tensor;
+    page-locked memory overlaps the copies) -> host peaks, via
+    spx_fft_peaks_host.  Returns (int32 [beams, R, 8] MaxValue words, counts
+    [beams]) as CPU tensors, written into out / counts when given."""
+    torch = _torch()
+    if isinstance(x, np.ndarray):
+        x = torch.from_numpy(np.ascontiguousarray(x, dtype=np.complex64))
+    if x.is_cuda or x.dtype != torch.complex64 or not x.is_contiguous():
+        raise ValueError("x must be a contiguous host complex64 tensor or array")
+    x2 = x.reshape(-1, x.shape[-1])
+    beams, n_point = x2.shape
+    if mode in (PEAK_ONE, PEAK_TWO):
+        per = 4 if mode == PEAK_ONE else 8
+    elif mode == PEAK_ALL:
+        per = _capi.all_maxima_capacity(nfft, search_start, search_end, max_per_beam)[2]
+    else:
+        per = max_per_beam
+    if out is None:
+        out = torch.zeros((beams, per, 8), dtype=torch.int32)
+    if counts is None:
+        counts = torch.zeros(beams, dtype=torch.int32)
+    if out.is_cuda or out.numel() < beams * per * 8 or counts.is_cuda or counts.numel() < beams:
+        raise ValueError("out / counts must be host tensors of [beams, R, 8] / [beams]")
+    p = peak_params(mode, search_start, search_end, search_range, max_per_beam, refine,
+                    sample_rate, thresh_sigma)
+    c = ctx or default_context()
+    c.bind_stream()
+    c.check(lib.spx_fft_peaks_host(c.h, _ptr(x2), beams, n_point, nfft, window, C.byref(p), _ptr(out),
+                                   _ptr(counts)))
+    return out, counts
+
+
 def next_pow2(n: int) -> int:
     return int(lib.spx_next_pow2(n))
 

@@ -87,6 +87,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_topk": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_fft_peaks": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_all_maxima_noalloc": (_i, [_vp, _vp, _vp, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
+    "spx_fft_peaks_host": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, C.POINTER(SpxPeakParams), _vp, _vp]),
     "spx_batch_create": (_i, [_vp, _u32, _vp, _vp, _u32, C.POINTER(SpxPeakParams), C.POINTER(_vp)]),
     "spx_batch_destroy": (_i, [_vp]),
     "spx_batch_input_samples": (_u64, [_vp]),

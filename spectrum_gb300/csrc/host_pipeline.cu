@@ -1,0 +1,132 @@
+// host_pipeline.cu — spx_fft_peaks_host: raw samples in host memory -> peaks
+// in host memory, the path of SpectrumProcessorROCm::ProcessFromCPU /
+// FindAllMaximaFromCPU (src/fft_func/src/spectrum_processor_rocm.cpp:444-500:
+// upload, FFT, peak search, read back).
+//
+// The beams go through in chunks of about kChunkBytes of samples on three
+// streams: copy-in (host -> device), the context's stream (the fused
+// spx_fft_peaks launch) and copy-out (device -> host), so the upload of chunk
+// i + 1 overlaps the transform of chunk i and the read-back of chunk i - 1.
+// Staging: three input slots and two output slots in one device buffer owned
+// by the context.  Events order slot reuse:
+//   copy-in of chunk i waits until chunk i - 3 was computed (its input slot);
+//   compute of chunk i waits for its upload and for the read-back of chunk
+//   i - 2 (its output slot).
+// With pageable host memory the copies are still correct but do not overlap.
+#include <algorithm>
+#include <cstring>
+
+#include "spx_internal.h"
+
+using namespace spx;
+
+namespace {
+
+constexpr size_t kChunkBytes = size_t(16) << 20;
+constexpr int kInSlots = 3, kOutSlots = 2;
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+spx_status ensure_pipeline(spx_ctx* ctx, size_t bytes, size_t n_events) {
+  cudaError_t e = cudaSuccess;
+  if (!ctx->copy_in) e = cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !ctx->copy_out) e = cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: stream creation");
+  if (ctx->stage_bytes < bytes) {
+    if (ctx->d_stage) cudaFree(ctx->d_stage);
+    ctx->d_stage = nullptr;
+    ctx->stage_bytes = 0;
+    e = cudaMalloc(&ctx->d_stage, bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: staging buffer");
+    ctx->stage_bytes = bytes;
+  }
+  while (ctx->events.size() < n_events) {
+    cudaEvent_t ev;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: event creation");
+    ctx->events.push_back(ev);
+  }
+  return SPX_OK;
+}
+
+}  // namespace
+
+extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
+                                         uint32_t n_point, uint32_t nfft, uint32_t window,
+                                         const spx_peak_params* params, spx_max_value* h_out,
+                                         uint32_t* h_counts) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (!params) return fail(ctx, SPX_ERR_INVALID_ARG, "params is null");
+  if (params->mode > SPX_PEAK_TOPK)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "unknown peak mode " + std::to_string(params->mode));
+  if (beams == 0) return SPX_OK;
+  if (!h_in || !h_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: null host pointer");
+  if (n_point == 0 || nfft < n_point)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: need 0 < n_point <= nfft");
+  const bool counted = params->mode == SPX_PEAK_ALL || params->mode == SPX_PEAK_TOPK;
+  if (counted && !h_counts) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: counts is null");
+  // rows per beam in the output
+  uint32_t per = 0;
+  switch (params->mode) {
+    case SPX_PEAK_ONE: per = 4; break;
+    case SPX_PEAK_TWO: per = 8; break;
+    case SPX_PEAK_ALL: {
+      uint32_t s = 0, e = 0;
+      spx_all_maxima_capacity(nfft, params->search_start, params->search_end, params->max_per_beam, &s, &e, &per);
+      break;
+    }
+    default: per = params->max_per_beam; break;
+  }
+  DeviceGuard guard(ctx->device);
+  const size_t beam_in = (size_t)n_point * sizeof(float2);
+  const uint32_t cb = (uint32_t)std::max<size_t>(1, std::min<size_t>(beams, kChunkBytes / beam_in));
+  const uint32_t nchunks = (beams + cb - 1) / cb;
+  const size_t in_slot = align_up((size_t)cb * beam_in, 256);
+  const size_t out_slot = align_up((size_t)cb * std::max<uint32_t>(per, 1) * sizeof(spx_max_value), 256);
+  const size_t cnt_slot = align_up((size_t)cb * sizeof(uint32_t), 256);
+  const size_t total = kInSlots * in_slot + kOutSlots * (out_slot + cnt_slot);
+  spx_status st = ensure_pipeline(ctx, total, (size_t)3 * nchunks);
+  if (st != SPX_OK) return st;
+  char* base = static_cast<char*>(ctx->d_stage);
+  auto in_ptr = [&](uint32_t i) { return base + (i % kInSlots) * in_slot; };
+  auto out_ptr = [&](uint32_t i) { return base + kInSlots * in_slot + (i % kOutSlots) * (out_slot + cnt_slot); };
+  cudaEvent_t* ev_in = ctx->events.data();
+  cudaEvent_t* ev_comp = ev_in + nchunks;
+  cudaEvent_t* ev_out = ev_comp + nchunks;
+  // the staging buffer may still be read by work queued before this call
+  cudaError_t e = cudaEventRecord(ev_comp[0], ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_in, ev_comp[0], 0);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: ordering");
+  const char* src = static_cast<const char*>(h_in);
+  for (uint32_t i = 0; i < nchunks; ++i) {
+    const uint32_t b0 = i * cb, nb = std::min(cb, beams - b0);
+    if (i >= (uint32_t)kInSlots) e = cudaStreamWaitEvent(ctx->copy_in, ev_comp[i - kInSlots], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(in_ptr(i), src + (size_t)b0 * beam_in, (size_t)nb * beam_in, cudaMemcpyHostToDevice,
+                          ctx->copy_in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_in[i], ctx->copy_in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ev_in[i], 0);
+    if (e == cudaSuccess && i >= (uint32_t)kOutSlots) e = cudaStreamWaitEvent(ctx->stream, ev_out[i - kOutSlots], 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: upload");
+    char* o = out_ptr(i);
+    uint32_t* c = reinterpret_cast<uint32_t*>(o + out_slot);
+    st = spx_fft_peaks(ctx, in_ptr(i), nb, n_point, nfft, window, params, reinterpret_cast<spx_max_value*>(o),
+                       counted ? c : nullptr);
+    if (st != SPX_OK) {
+      cudaStreamSynchronize(ctx->copy_in);
+      return st;
+    }
+    e = cudaEventRecord(ev_comp[i], ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_out, ev_comp[i], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h_out + (size_t)b0 * per, o, (size_t)nb * per * sizeof(spx_max_value),
+                          cudaMemcpyDeviceToHost, ctx->copy_out);
+    if (e == cudaSuccess && counted)
+      e = cudaMemcpyAsync(h_counts + b0, c, (size_t)nb * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->copy_out);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_out[i], ctx->copy_out);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: read-back");
+  }
+  e = cudaStreamSynchronize(ctx->copy_out);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: synchronize");
+  return spx_synchronize(ctx);
+}

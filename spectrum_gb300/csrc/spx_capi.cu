@@ -137,6 +137,16 @@ spx_status spx_destroy(spx_ctx* ctx) {
     for (int i = 0; i < 4; ++i)
       if (ctx->d_scratch[i]) cudaFree(ctx->d_scratch[i]);
     if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->copy_in) {
+      cudaStreamSynchronize(ctx->copy_in);
+      cudaStreamDestroy(ctx->copy_in);
+    }
+    if (ctx->copy_out) {
+      cudaStreamSynchronize(ctx->copy_out);
+      cudaStreamDestroy(ctx->copy_out);
+    }
+    if (ctx->d_stage) cudaFree(ctx->d_stage);
+    for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
   }
   delete ctx;
   return SPX_OK;

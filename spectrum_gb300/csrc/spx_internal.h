@@ -8,6 +8,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "spx.h"
 #include "spx_geom.h"
@@ -47,6 +48,11 @@ struct spx_ctx {
   size_t scratch_bytes[4] = {0, 0, 0, 0};
   uint32_t* d_error = nullptr;         // device error word (kErr* bits)
   uint32_t epoch = 0;                  // lookback status epoch
+  // Host-buffer pipeline (spx_fft_peaks_host): copy streams, staging, events.
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  std::vector<cudaEvent_t> events;
 };
 
 namespace spx {

@@ -110,3 +110,36 @@ def test_fused_large_workload_properties(spx, cuda):
             isolated = np.sort(others)[1] > 16.0 / nfft if len(fr) > 1 else True
             if a >= 0.5 * max(bs.amps[b]) and isolated:
                 assert np.min(np.abs(f - ft)) < 2.0 / nfft
+
+
+@pytest.mark.parametrize("nfft,n_point,beams,mode,k,sigma,pinned", [
+    (131072, 65536, 70, "all", 1000, 6.0, True),    # 3 chunks of 32 beams (last partial)
+    (4096, 4096, 2600, "topk", 5, 0.0, True),      # 6 chunks: input and output slots reused
+    (4096, 4000, 1100, "one", 0, 0.0, False),      # pageable numpy input, ONE_PEAK (no counts)
+])
+def test_fft_peaks_host_matches_device_path(spx, cuda, nfft, n_point, beams, mode, k, sigma, pinned):
+    """spx_fft_peaks_host (host in, host out, chunked copy/compute overlap)
+    returns exactly what spx_fft_peaks returns on the same samples."""
+    import torch
+    from spectrum_gb300 import synth
+    bs = synth.make_beams([n_point] * beams, tones=(1, 8), snr_db=(0.0, 40.0), seed=nfft + beams)
+    xd = synth.synth_torch(bs, device=cuda)
+    m = {"all": spx.PEAK_ALL, "topk": spx.PEAK_TOPK, "one": spx.PEAK_ONE}[mode]
+    kw = dict(sample_rate=1000.0, refine=spx.REFINE_PARABOLIC, thresh_sigma=sigma)
+    if mode != "one":
+        kw["max_per_beam"] = k
+    od, cd = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, m, **kw)
+    xh = xd.cpu()
+    if pinned:
+        xh = xh.pin_memory()
+    else:
+        xh = xh.numpy()
+    oh, ch = spx.fft_peaks_host(xh, nfft, spx.WINDOW_HANN, m, **kw)
+    gd, gh = spx.maxvalues_to_numpy(od), spx.maxvalues_to_numpy(oh)
+    if mode == "one":
+        np.testing.assert_array_equal(gh, gd)
+        return
+    cd = cd.cpu().numpy()
+    np.testing.assert_array_equal(ch.numpy(), cd)
+    for b in range(beams):
+        np.testing.assert_array_equal(gh[b, : cd[b]], gd[b, : cd[b]])
