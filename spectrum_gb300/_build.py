@@ -42,12 +42,12 @@ def _flags(ptxas_verbose: bool) -> list[str]:
 
 
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _compile_one(src: Path, ptxas_verbose: bool) -> tuple[Path, str]:
     obj = BUILD / (src.stem + ".o")
-    deps = [src] + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "spx.h"]
+    deps = [src] + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").rglob("*.h*"))
     if obj.exists() and not ptxas_verbose:
         t = obj.stat().st_mtime
         if all(d.stat().st_mtime <= t for d in deps if d.exists()):
