@@ -144,6 +144,14 @@ const char* spx_last_error(const spx_ctx* ctx);
 const char* spx_status_string(spx_status status);
 int spx_abi_version(void);
 
+/* Self-test of the bounded device-side waits (no reference counterpart).
+ * Every spin-wait in this library's kernels (the look-back of the all-maxima
+ * scan) gives up after 1 s, sets the context's error word and lets the kernel
+ * finish; the next spx_synchronize returns SPX_ERR_TIMEOUT and clears it.
+ * This call runs one such wait on a predecessor that never publishes, so it
+ * takes about 1 s and returns SPX_ERR_TIMEOUT; the context stays usable. */
+spx_status spx_selftest_wait_timeout(spx_ctx* ctx);
+
 /* ---- sizes -------------------------------------------------------------- */
 /* nextPow2(n) as the reference computes it (fft_processor_rocm.cpp:665-671); 0 -> 1. */
 uint32_t spx_next_pow2(uint32_t n);

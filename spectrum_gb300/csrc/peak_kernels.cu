@@ -379,6 +379,26 @@ all_maxima_kernel(AmArgs a) {
   }
 }
 
+// Self-test of the bounded wait: one thread waits, as tile 1 of a beam, on
+// tile 0's status word, which holds another epoch and is never published, so
+// the wait ends at its time bound and sets kErrLookbackTimeout.
+__global__ void lookback_timeout_probe_kernel(unsigned long long* status, uint32_t* err, uint32_t epoch) {
+  AmArgs a{};
+  a.status = status;
+  a.err = err;
+  a.tiles_per_beam = 2;
+  a.epoch = epoch;
+  lookback(a, 0, 1, 0);
+}
+
+spx_status launch_lookback_timeout_probe(spx_ctx* ctx, unsigned long long* d_status) {
+  cudaError_t e = cudaMemsetAsync(d_status, 0, 2 * sizeof(unsigned long long), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "lookback probe memset");
+  lookback_timeout_probe_kernel<<<1, 1, 0, ctx->stream>>>(d_status, ctx->d_error, 1u);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch lookback_timeout_probe_kernel");
+}
+
 spx_status launch_all_maxima(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
                              uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
                              uint32_t cap, float fs, uint32_t refine, const float* d_thr,

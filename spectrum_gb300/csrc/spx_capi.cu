@@ -178,6 +178,17 @@ spx_status spx_synchronize(spx_ctx* ctx) {
   return SPX_OK;
 }
 
+spx_status spx_selftest_wait_timeout(spx_ctx* ctx) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  void* st = nullptr;
+  spx_status s = get_scratch(ctx, kSlotWork, 2 * sizeof(unsigned long long), &st);
+  if (s != SPX_OK) return s;
+  s = launch_lookback_timeout_probe(ctx, static_cast<unsigned long long*>(st));
+  if (s != SPX_OK) return s;
+  return spx_synchronize(ctx);
+}
+
 uint32_t spx_next_pow2(uint32_t n) {
   if (n == 0) return 1;
   n--;

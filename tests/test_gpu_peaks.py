@@ -186,3 +186,26 @@ def test_fft_peaks_matches_oracle_on_same_spectrum(spx, cuda, mode):
 def test_status_word_clean_after_runs(spx, cuda):
     """No bounded device wait expired during the tests above."""
     spx.default_context().synchronize()
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(spx, cuda):
+    """A look-back wait on a status word nothing publishes gives up after its
+    1 s bound: the call reports SPX_ERR_TIMEOUT, the error word is cleared,
+    and the same context then runs an all-maxima search correctly."""
+    import time
+
+    import torch
+    ctx = spx.default_context()
+    ctx.bind_stream()
+    t0 = time.perf_counter()
+    st = spx.lib.spx_selftest_wait_timeout(ctx.h)
+    dt = time.perf_counter() - t0
+    assert st == spx._capi.SPX_ERR_TIMEOUT
+    assert 0.9 < dt < 30.0
+    assert b"bounded device-side wait" in spx.lib.spx_last_error(ctx.h)
+    assert spx.lib.spx_synchronize(ctx.h) == spx._capi.SPX_OK
+    rng = np.random.default_rng(3)
+    z = (rng.standard_normal((4, 8192)) + 1j * rng.standard_normal((4, 8192))).astype(np.complex64)
+    out, counts = spx.all_maxima(torch.from_numpy(z).to(cuda), sample_rate=1.0)
+    ref, rc = orc.all_maxima(None, z, 8192, 1.0)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
