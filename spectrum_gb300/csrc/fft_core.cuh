@@ -164,6 +164,41 @@ SPX_DEV void cross_stage_exchange(float2* __restrict__ slot, uint32_t c, uint32_
   }
 }
 
+// Starts asynchronous L2 fills of the 16-byte granules lying entirely in
+// [p, p + bytes), in 16 KB pieces spread over threads tid, tid + T, ...
+// (cp.async.bulk.prefetch: no result, no ordering; the range must be valid
+// device memory).
+SPX_DEV void prefetch_l2(const void* p, size_t bytes, uint32_t tid, uint32_t T) {
+  constexpr uintptr_t kPiece = 16384;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t lo = (a + 15) & ~(uintptr_t)15;
+  const uintptr_t hi = (a + bytes) & ~(uintptr_t)15;
+  for (uintptr_t x = lo + (uintptr_t)tid * kPiece; x < hi; x += (uintptr_t)T * kPiece) {
+    const uint32_t n = (uint32_t)min(kPiece, hi - x);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(x), "r"(n) : "memory");
+  }
+}
+
+// Prefetch into L2 of the samples of beam `beam + g.ahead` that this CTA
+// will read when it runs that beam's turn one residency wave later: the whole
+// beam (C == 1) or, for rank c of a cluster, the C slices [n1 M + c S,
+// n1 M + c S + S) of its cross stage.
+SPX_DEV void prefetch_future_beam(const FftGeom& g, const float2* in, uint32_t n_point, uint32_t beam,
+                                  uint32_t c, uint32_t tid, uint32_t T) {
+  if (g.ahead == 0 || beam + g.ahead >= g.beams) return;
+  const float2* x = in + (size_t)(beam + g.ahead) * n_point;
+  if (g.C == 1) {
+    prefetch_l2(x, (size_t)n_point * sizeof(float2), tid, T);
+    return;
+  }
+  const uint32_t S = (g.M + g.C - 1) / g.C;
+  if (tid < g.C) {
+    const uint32_t lo = tid * g.M + c * S;
+    const uint32_t hi = min(min(lo + S, (tid + 1) * g.M), n_point);
+    if (lo < hi) prefetch_l2(x + lo, (size_t)(hi - lo) * sizeof(float2), 0, 1);
+  }
+}
+
 // Invalidates (without write-back) every 128-byte L2 line lying entirely in
 // [p, p + bytes); lines shared with a neighbouring row are left alone.
 SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_t T) {

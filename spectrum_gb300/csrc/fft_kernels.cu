@@ -9,7 +9,9 @@
 // each beam reads its n_point samples once and writes its spectrum once.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <set>
 #include <utility>
 #include <vector>
@@ -30,6 +32,7 @@ fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __r
   extern __shared__ float2 s[];
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   const uint32_t beam = blockIdx.x;
+  prefetch_future_beam(g, in, n_point, beam, 0, tid, T);
   first_pass_dispatch<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tid, T);
   local_passes<EPT>(s, g, 1, tw_local, tid, T);
   epilogue_out(s, g, 0, beam, out, out_mode, scale, tid, T);
@@ -57,6 +60,7 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
   const uint32_t beam = blockIdx.x / g.C;
   float2* slot = xch + (size_t)beam * g.nfft;
   const SampleLoader ld{in + (size_t)beam * n_point, n_point, win};
+  prefetch_future_beam(g, in, n_point, beam, c, tid, T);
   switch (g.C) {
     case 2: cross_stage_exchange<2>(slot, c, g.M, ld, tw_cross, tid, T); break;
     case 3: cross_stage_exchange<3>(slot, c, g.M, ld, tw_cross, tid, T); break;
@@ -260,11 +264,54 @@ cudaError_t configure_kernel(const void* kernel, size_t max_smem) {
   return cudaSuccess;
 }
 
+// Beams resident at once for a launch of `kernel` with geometry g (blocks
+// per SM times SMs, or active clusters), cached per (device, kernel, shape):
+// the L2 prefetch distance of prefetch_future_beam.
+uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void*, uint32_t, uint32_t, size_t>, uint32_t> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const auto key = std::make_tuple(dev, kernel, g.T, g.C, smem);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  uint32_t n = 0;
+  if (g.C == 1) {
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)g.T, smem) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      n = (uint32_t)(per_sm * sms);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.C, 1, 1);
+    cfg.blockDim = dim3(g.T, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = g.C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) == cudaSuccess) n = (uint32_t)clusters;
+  }
+  cudaGetLastError();
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = n;
+  return n;
+}
+
 template <typename K>
-static cudaError_t launch_beams(K kernel, const FftGeom& g, uint32_t beams, size_t smem,
+static cudaError_t launch_beams(K kernel, FftGeom& g, uint32_t beams, size_t smem,
                                 cudaStream_t stream, void** args) {
   cudaError_t e0 = configure_kernel((const void*)kernel, kMaxLocal * sizeof(float2) + 16384);
   if (e0 != cudaSuccess) return e0;
+  g.beams = beams;
+  g.ahead = resident_beams((const void*)kernel, g, smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(beams * g.C, 1, 1);
   cfg.blockDim = dim3(g.T, 1, 1);

@@ -391,6 +391,7 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
   if (g.C == 1) {
     const uint32_t beam = blockIdx.x;
+    prefetch_future_beam(g, a.in, a.n_point, beam, 0, tid, T);
     first_pass_dispatch<EPT>(s, g, SampleLoader{a.in + (size_t)beam * a.n_point, a.n_point, a.win},
                              tid, T);
     local_passes<EPT>(s, g, 1, a.tw_local, tid, T);
@@ -402,6 +403,7 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   const uint32_t beam = blockIdx.x / g.C;
   float2* slot = a.xch + (size_t)beam * g.nfft;
   const SampleLoader ld{a.in + (size_t)beam * a.n_point, a.n_point, a.win};
+  prefetch_future_beam(g, a.in, a.n_point, beam, c, tid, T);
   switch (g.C) {
     case 2: cross_stage_exchange<2>(slot, c, g.M, ld, a.tw_cross, tid, T); break;
     case 3: cross_stage_exchange<3>(slot, c, g.M, ld, a.tw_cross, tid, T); break;
@@ -478,6 +480,8 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   const void* kfn = g.ept == 32 ? (const void*)fft_peaks_kernel<32> : (const void*)fft_peaks_kernel<16>;
   e = configure_kernel(kfn, 227 * 1024);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
+  g.beams = beams;
+  g.ahead = resident_beams(kfn, g, smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(beams * g.C, 1, 1);
   cfg.blockDim = dim3(g.T, 1, 1);

@@ -24,6 +24,10 @@ struct FftGeom {
   uint32_t radix[kMaxPass];
   uint32_t ns[kMaxPass];
   uint32_t twoff[kMaxPass];
+  // Set per launch (0 in plans): beams in the launch and the L2 prefetch
+  // distance in beams (the beams resident at once; 0 = no prefetch).
+  uint32_t beams;
+  uint32_t ahead;
 };
 
 }  // namespace spx

@@ -143,3 +143,40 @@ def test_fft_peaks_host_matches_device_path(spx, cuda, nfft, n_point, beams, mod
     np.testing.assert_array_equal(ch.numpy(), cd)
     for b in range(beams):
         np.testing.assert_array_equal(gh[b, : cd[b]], gd[b, : cd[b]])
+
+
+def _tie_inputs(n):
+    """Inputs whose spectra are full of exact magnitude ties and plateaus."""
+    rng = np.random.default_rng(n)
+    imp = np.zeros((1, n), np.complex64)
+    imp[0, 0] = 1.0                       # flat |X| = 1 everywhere
+    two = np.zeros((1, n), np.complex64)
+    two[0, 0], two[0, 3] = 1.0, 1.0       # |1 + e^{-i 2 pi 3k/N}|: repeating exact values
+    dc = np.ones((1, n), np.complex64)    # one line at k = 0
+    ints = (rng.integers(-2, 3, (3, n)) + 1j * rng.integers(-2, 3, (3, n))).astype(np.complex64)
+    return np.concatenate([imp, two, dc, ints])
+
+
+@pytest.mark.parametrize("nfft", [4096, 65536, 131072])
+@pytest.mark.parametrize("sigma", [0.0, 6.0])
+def test_fused_exact_ties(spx, cuda, nfft, sigma):
+    """Magnitude comparisons and the noise histogram take the exact square
+    root whenever two |X|^2 are too close to decide from |X|^2 alone: spectra
+    with exact ties and plateaus give the oracle's lists bit for bit."""
+    import torch
+    if nfft > 16384 and sigma == 0.0:
+        pytest.skip("unthresholded all-maxima with C > 1 runs the composed path")
+    x = _tie_inputs(min(nfft, 65536))
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_NONE, spx.PEAK_ALL, sample_rate=1.0,
+                                refine=1, thresh_sigma=sigma)
+    ref, rc = orc.all_maxima(None, spec, nfft, 1.0, refine=1, thresh_sigma=sigma)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+    if nfft <= 16384:
+        out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_NONE, spx.PEAK_TOPK, sample_rate=1.0,
+                                    max_per_beam=8, refine=1, thresh_sigma=sigma)
+        ref, rc = orc.topk(None, spec, nfft, 1.0, 8, thresh_sigma=sigma)
+        np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+        assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
