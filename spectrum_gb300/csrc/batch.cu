@@ -100,10 +100,19 @@ template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ beams,
                  const BatchCta* __restrict__ ctas, const BatchGeom* __restrict__ geoms,
-                 uint32_t window, float2* __restrict__ xch, float2* __restrict__ spec) {
+                 uint32_t window, float2* __restrict__ xch, float2* __restrict__ spec,
+                 uint32_t ahead) {
   extern __shared__ float2 s[];
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t tid = threadIdx.x, T = blockDim.x;
+  // L2 prefetch for the CTA that starts one residency wave (`ahead` CTAs) later
+  if (ahead && blockIdx.x + ahead < gridDim.x) {
+    const BatchCta f = ctas[blockIdx.x + ahead];
+    if (f.beam != kIdle) {
+      const BatchBeam fb = beams[f.beam];
+      prefetch_beam_part(in + fb.in_off, fb.n_point, geoms[fb.geom].g.C, geoms[fb.geom].g.M, f.c, tid, T);
+    }
+  }
   const BatchCta d = ctas[blockIdx.x];
   const bool active = d.beam != kIdle;
   BatchBeam bm{};
@@ -373,8 +382,9 @@ spx_status launch_set(spx_ctx* ctx, spx_batch* b, const LaunchSet& ls, const voi
   uint32_t window = b->window;
   float2* xch = b->d_xch;
   float2* spec = b->d_spec;
+  uint32_t ahead = resident_ctas(kfn, ls.threads, ls.smem, ls.cluster);
   void* args[] = {(void*)&in, (void*)&beams, (void*)&ctas, (void*)&geoms,
-                  (void*)&window, (void*)&xch, (void*)&spec};
+                  (void*)&window, (void*)&xch, (void*)&spec, (void*)&ahead};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(ls.n_ctas, 1, 1);
   cfg.blockDim = dim3(ls.threads, 1, 1);

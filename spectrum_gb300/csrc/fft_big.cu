@@ -25,11 +25,20 @@ constexpr uint32_t kBigM = 16384;
 template <int CB>
 __global__ void __launch_bounds__(256)
 big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
-                const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch) {
+                const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch,
+                uint32_t ahead) {
   __shared__ float2 tile[CB][33];
   const uint32_t tid = threadIdx.x;
   const uint32_t beam = blockIdx.y, n2_0 = blockIdx.x * 32;
   const float2* x = in + (size_t)beam * n_point;
+  {  // L2 prefetch of the 32-column tile of the CTA `ahead` places later
+    const uint64_t f = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x + ahead;
+    if (ahead && f < (uint64_t)gridDim.x * gridDim.y && tid < CB) {
+      const uint32_t fb = (uint32_t)(f / gridDim.x), fc = (uint32_t)(f % gridDim.x) * 32;
+      const uint32_t lo = tid * kBigM + fc, hi = min(lo + 32, n_point);
+      if (lo < hi) prefetch_l2(in + (size_t)fb * n_point + lo, (size_t)(hi - lo) * sizeof(float2), 0, 1);
+    }
+  }
   for (uint32_t e = tid; e < CB * 32; e += 256) {
     const uint32_t n1 = e >> 5, col = e & 31;
     tile[n1][col] = load_sample(x, n1 * kBigM + n2_0 + col, n_point, win);
@@ -76,6 +85,8 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, const float2* __
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   const uint32_t beam = blockIdx.x / g.C, k1 = blockIdx.x % g.C;
   const float2* row = scratch + (size_t)beam * g.nfft + (size_t)k1 * g.M;
+  if (g.ahead && blockIdx.x + g.ahead < gridDim.x)  // the row the CTA one wave later reads
+    prefetch_l2(row + (size_t)g.ahead * g.M, (size_t)g.M * sizeof(float2), tid, T);
   first_pass_dispatch<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tid, T);
   local_passes<EPT>(s, g, 1, tw_local, tid, T);
   epilogue_out(s, g, k1, beam, out, out_mode, scale, tid, T);
@@ -125,16 +136,22 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   if (st != SPX_OK) return st;
   float2* scratch = static_cast<float2*>(scr);
   dim3 grid(kBigM / 32, beams);
+  const void* kcols = g.C == 64 ? (const void*)big_cols_kernel<64> : (const void*)big_cols_kernel<32>;
+  const uint32_t ahead_cols = resident_ctas(kcols, 256, 0, 1);
   if (g.C == 64)
-    big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch);
+    big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
+                                                       ahead_cols);
   else
-    big_cols_kernel<32><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch);
+    big_cols_kernel<32><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
+                                                       ahead_cols);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
   const void* kfn = (const void*)big_rows_kernel<kEPTDefault>;
   e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows_kernel");
   FftGeom gg = g;
+  gg.beams = beams;
+  gg.ahead = resident_ctas(kfn, g.T, (size_t)g.Mpad * sizeof(float2), 1);
   const float2* twl = plan.d_tw_local;
   const float2* sc = scratch;
   void* args[] = {(void*)&gg, (void*)&twl, (void*)&sc, (void*)&d_out, (void*)&out_mode, (void*)&scale};

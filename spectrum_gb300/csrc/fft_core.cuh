@@ -183,20 +183,26 @@ SPX_DEV void prefetch_l2(const void* p, size_t bytes, uint32_t tid, uint32_t T) 
 // will read when it runs that beam's turn one residency wave later: the whole
 // beam (C == 1) or, for rank c of a cluster, the C slices [n1 M + c S,
 // n1 M + c S + S) of its cross stage.
-SPX_DEV void prefetch_future_beam(const FftGeom& g, const float2* in, uint32_t n_point, uint32_t beam,
-                                  uint32_t c, uint32_t tid, uint32_t T) {
-  if (g.ahead == 0 || beam + g.ahead >= g.beams) return;
-  const float2* x = in + (size_t)(beam + g.ahead) * n_point;
-  if (g.C == 1) {
+// The samples of an n_point-sample beam x that rank c of its C CTAs reads
+// first (the whole beam for C == 1, the cross-stage slices otherwise).
+SPX_DEV void prefetch_beam_part(const float2* x, uint32_t n_point, uint32_t C, uint32_t M, uint32_t c,
+                                uint32_t tid, uint32_t T) {
+  if (C == 1) {
     prefetch_l2(x, (size_t)n_point * sizeof(float2), tid, T);
     return;
   }
-  const uint32_t S = (g.M + g.C - 1) / g.C;
-  if (tid < g.C) {
-    const uint32_t lo = tid * g.M + c * S;
-    const uint32_t hi = min(min(lo + S, (tid + 1) * g.M), n_point);
+  const uint32_t S = (M + C - 1) / C;
+  if (tid < C) {
+    const uint32_t lo = tid * M + c * S;
+    const uint32_t hi = min(min(lo + S, (tid + 1) * M), n_point);
     if (lo < hi) prefetch_l2(x + lo, (size_t)(hi - lo) * sizeof(float2), 0, 1);
   }
+}
+
+SPX_DEV void prefetch_future_beam(const FftGeom& g, const float2* in, uint32_t n_point, uint32_t beam,
+                                  uint32_t c, uint32_t tid, uint32_t T) {
+  if (g.ahead == 0 || beam + g.ahead >= g.beams) return;
+  prefetch_beam_part(in + (size_t)(beam + g.ahead) * n_point, n_point, g.C, g.M, c, tid, T);
 }
 
 // Invalidates (without write-back) every 128-byte L2 line lying entirely in

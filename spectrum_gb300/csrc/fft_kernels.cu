@@ -264,45 +264,49 @@ cudaError_t configure_kernel(const void* kernel, size_t max_smem) {
   return cudaSuccess;
 }
 
-// Beams resident at once for a launch of `kernel` with geometry g (blocks
-// per SM times SMs, or active clusters), cached per (device, kernel, shape):
-// the L2 prefetch distance of prefetch_future_beam.
-uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem) {
+// CTAs of a launch of `kernel` resident at once (blocks per SM times SMs,
+// or active clusters times the cluster size), cached per (device, kernel,
+// shape): the L2 prefetch distance of the FFT kernels.
+uint32_t resident_ctas(const void* kernel, uint32_t threads, size_t smem, uint32_t cluster) {
   static std::mutex mu;
   static std::map<std::tuple<int, const void*, uint32_t, uint32_t, size_t>, uint32_t> cache;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  const auto key = std::make_tuple(dev, kernel, g.T, g.C, smem);
+  const auto key = std::make_tuple(dev, kernel, threads, cluster, smem);
   {
     std::lock_guard<std::mutex> lock(mu);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
   }
   uint32_t n = 0;
-  if (g.C == 1) {
+  if (cluster <= 1) {
     int per_sm = 0, sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)g.T, smem) == cudaSuccess &&
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)threads, smem) == cudaSuccess &&
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
       n = (uint32_t)(per_sm * sms);
   } else {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g.C, 1, 1);
-    cfg.blockDim = dim3(g.T, 1, 1);
+    cfg.gridDim = dim3(cluster, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = g.C;
+    attr[0].val.clusterDim.x = cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int clusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) == cudaSuccess) n = (uint32_t)clusters;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) == cudaSuccess) n = (uint32_t)clusters * cluster;
   }
   cudaGetLastError();
   std::lock_guard<std::mutex> lock(mu);
   cache[key] = n;
   return n;
+}
+
+uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem) {
+  return resident_ctas(kernel, g.T, smem, g.C) / g.C;
 }
 
 template <typename K>

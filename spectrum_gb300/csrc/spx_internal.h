@@ -124,7 +124,9 @@ spx_status launch_topk(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
                        uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
                        uint32_t k, float fs, uint32_t refine, const float* d_thr,
                        spx_max_value* d_out, uint32_t* d_counts);
-// Beams of a launch of `kernel` resident at once (the L2 prefetch distance).
+// CTAs (or beams of geometry g) of a launch of `kernel` resident at once:
+// the L2 prefetch distance of the FFT kernels.
+uint32_t resident_ctas(const void* kernel, uint32_t threads, size_t smem, uint32_t cluster);
 uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem);
 // Launches one bounded look-back wait that cannot be satisfied (self-test of
 // the timeout path); d_status: 2 words of scratch.
