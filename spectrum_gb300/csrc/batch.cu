@@ -70,7 +70,7 @@ struct SampleLoaderOTF {
   SPX_DEV float2 operator()(uint32_t n) const {
     float2 a = make_float2(0.f, 0.f);
     if (n < n_point) {
-      a = __ldg(x + n);
+      a = ld_stream(x + n);
       const float w = window_on_the_fly(kind, n, n_point);
       a.x *= w;
       a.y *= w;

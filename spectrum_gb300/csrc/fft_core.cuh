@@ -44,12 +44,20 @@ SPX_DEV uint32_t mod_ns(uint32_t j, uint32_t Ns) {
   return ((Ns & (Ns - 1)) == 0) ? (j & (Ns - 1)) : (j % Ns);
 }
 
+// Read-only load of a sample that is used once: not allocated in L1, so the
+// stream of samples does not evict the twiddle tables the passes reuse.
+SPX_DEV float2 ld_stream(const float2* p) {
+  float2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+
 // Sample n of a beam: window applied, zero beyond n_point.
 SPX_DEV float2 load_sample(const float2* __restrict__ x, uint32_t n,
                            uint32_t n_point, const float* __restrict__ win) {
   float2 a = make_float2(0.f, 0.f);
   if (n < n_point) {
-    a = __ldg(x + n);
+    a = ld_stream(x + n);
     if (win) {
       float w = __ldg(win + n);
       a.x *= w;
