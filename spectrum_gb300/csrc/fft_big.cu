@@ -87,8 +87,7 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, const float2* __
   const float2* row = scratch + (size_t)beam * g.nfft + (size_t)k1 * g.M;
   if (g.ahead && blockIdx.x + g.ahead < gridDim.x)  // the row the CTA one wave later reads
     prefetch_l2(row + (size_t)g.ahead * g.M, (size_t)g.M * sizeof(float2), tid, T);
-  first_pass_dispatch<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tid, T);
-  local_passes<EPT>(s, g, 1, tw_local, tid, T);
+  local_fft<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tw_local, tid, T);
   epilogue_out(s, g, k1, beam, out, out_mode, scale, tid, T);
 }
 

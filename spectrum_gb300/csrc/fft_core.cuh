@@ -250,6 +250,104 @@ SPX_DEV void local_passes(float2* s, const FftGeom& g, uint32_t p0,
   p = run_radix<2, EPT>(s, g, p, tw_local, tid, T);
 }
 
+// ---------------------------------------------------------------------------
+// Compile-time plans for power-of-two local sizes (EPT = 16).  The radix
+// order, strides and twiddle offsets are those build_geom emits for M = 2^a
+// (an 8 first when a = 3 mod 4, then 16s, then a 4 or a 2 last), so the
+// plan's twiddle table is used unchanged and the results are bit-identical to
+// the runtime passes; only the index arithmetic becomes constant.
+// ---------------------------------------------------------------------------
+constexpr int p2_log2(int x) { return x <= 1 ? 0 : 1 + p2_log2(x / 2); }
+template <int M>
+constexpr int p2_npass() { return p2_log2(M) / 4 + (p2_log2(M) % 4 ? 1 : 0); }
+template <int M>
+constexpr int p2_radix(int p) {
+  return p2_log2(M) % 4 == 3 ? (p == 0 ? 8 : 16)
+                             : (p < p2_log2(M) / 4 ? 16 : (p2_log2(M) % 4 == 2 ? 4 : 2));
+}
+template <int M>
+constexpr int p2_ns(int p) { return p == 0 ? 1 : p2_ns<M>(p - 1) * p2_radix<M>(p - 1); }
+template <int M>
+constexpr int p2_twoff(int p) { return p == 0 ? 0 : p2_twoff<M>(p - 1) + p2_ns<M>(p - 1) * (p2_radix<M>(p - 1) - 1); }
+
+// First pass (Ns = 1) from device memory, M and the thread count T = M / 16 constant.
+template <int M, typename Load>
+SPX_DEV void p2_first(float2* s, const Load& load, uint32_t tid) {
+  constexpr int R = p2_radix<M>(0), T = M / 16, B = M / R, Q = 16 / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = load(j + r * B);
+    Dft<R>::run(v);
+    const uint32_t lo = j & 15u, base = j * R;  // sw(base + r) = base + (r ^ lo) for R = 16; general below
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[R == 16 ? base + ((uint32_t)r ^ lo) : sw(base + r)] = v[r];
+  }
+  __syncthreads();
+}
+
+// Pass P >= 1 in shared memory.
+template <int M, int P>
+SPX_DEV void p2_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
+  constexpr int R = p2_radix<M>(P), Ns = p2_ns<M>(P), T = M / 16, B = M / R, Q = 16 / R;
+  static_assert(Q * T * R == M, "every thread owns Q butterflies");
+  float2 v[Q][R];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    const uint32_t sj = sw(j);
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q][r] = s[(B % 256 == 0) ? sj + r * B : sw(j + r * B)];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    const uint32_t k = j & (Ns - 1);
+    const float2* t = tw + p2_twoff<M>(P) + k;
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+    Dft<R>::run(v[q]);
+    const uint32_t base = (j - k) * R + k;
+    const uint32_t sb = sw(base);
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[(Ns % 256 == 0) ? sb + r * Ns : sw(base + r * Ns)] = v[q][r];
+  }
+  __syncthreads();
+}
+
+template <int M, int P>
+SPX_DEV void p2_passes_from(float2* s, const float2* __restrict__ tw, uint32_t tid) {
+  if constexpr (P < p2_npass<M>()) {
+    p2_pass<M, P>(s, tw, tid);
+    p2_passes_from<M, P + 1>(s, tw, tid);
+  }
+}
+
+// Whole local FFT of M points (first pass from `load`), M in {4096, 8192, 16384}.
+template <int M, typename Load>
+SPX_DEV void p2_local_fft(float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
+  p2_first<M>(s, load, tid);
+  p2_passes_from<M, 1>(s, tw, tid);
+}
+
+// Runs the local FFT with the compile-time plan when g is a power-of-two
+// size it covers (EPT 16, one thread per 16 points), else the runtime
+// plan.  Returns after the last pass's barrier either way.
+template <int EPT, typename Load>
+SPX_DEV void local_fft(float2* s, const FftGeom& g, const Load& load, const float2* __restrict__ tw,
+                       uint32_t tid, uint32_t T) {
+  if constexpr (EPT == 16) {
+    if (g.M == 16384 && T == 1024) return p2_local_fft<16384>(s, load, tw, tid);
+    if (g.M == 8192 && T == 512) return p2_local_fft<8192>(s, load, tw, tid);
+    if (g.M == 4096 && T == 256) return p2_local_fft<4096>(s, load, tw, tid);
+  }
+  first_pass_dispatch<EPT>(s, g, load, tid, T);
+  local_passes<EPT>(s, g, 1, tw, tid, T);
+}
+
 // Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
 SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
                           void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,

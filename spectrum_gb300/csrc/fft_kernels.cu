@@ -33,8 +33,7 @@ fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __r
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   const uint32_t beam = blockIdx.x;
   prefetch_future_beam(g, in, n_point, beam, 0, tid, T);
-  first_pass_dispatch<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tid, T);
-  local_passes<EPT>(s, g, 1, tw_local, tid, T);
+  local_fft<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tw_local, tid, T);
   epilogue_out(s, g, 0, beam, out, out_mode, scale, tid, T);
 }
 
@@ -73,9 +72,8 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
   }
   cl.sync();
   const float2* row = slot + (size_t)c * g.M;
-  first_pass_dispatch<EPT>(s, g, ExchangeLoader{row}, tid, T);
+  local_fft<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T);
   discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
-  local_passes<EPT>(s, g, 1, tw_local, tid, T);
   epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
 }
 

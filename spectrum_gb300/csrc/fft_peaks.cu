@@ -392,9 +392,7 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   if (g.C == 1) {
     const uint32_t beam = blockIdx.x;
     prefetch_future_beam(g, a.in, a.n_point, beam, 0, tid, T);
-    first_pass_dispatch<EPT>(s, g, SampleLoader{a.in + (size_t)beam * a.n_point, a.n_point, a.win},
-                             tid, T);
-    local_passes<EPT>(s, g, 1, a.tw_local, tid, T);
+    local_fft<EPT>(s, g, SampleLoader{a.in + (size_t)beam * a.n_point, a.n_point, a.win}, a.tw_local, tid, T);
     peaks_single_cta(s, shist, s_red, g, beam, a);
     return;
   }
@@ -416,9 +414,8 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   }
   cl.sync();
   const float2* row = slot + (size_t)c * g.M;
-  first_pass_dispatch<EPT>(s, g, ExchangeLoader{row}, tid, T);
+  local_fft<EPT>(s, g, ExchangeLoader{row}, a.tw_local, tid, T);
   discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
-  local_passes<EPT>(s, g, 1, a.tw_local, tid, T);
   peaks_cluster(s, shist, s_red, shot, slist, kList, g, c, beam, a);
 }
 
