@@ -116,15 +116,12 @@ fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ be
   const BatchCta d = ctas[blockIdx.x];
   const bool active = d.beam != kIdle;
   BatchBeam bm{};
-  FftGeom g{};
-  const float2* twl = nullptr;
-  const float2* twc = nullptr;
-  if (active) {
-    bm = beams[d.beam];
-    g = geoms[bm.geom].g;
-    twl = geoms[bm.geom].twl;
-    twc = geoms[bm.geom].twc;
-  }
+  if (active) bm = beams[d.beam];
+  // the geometry is read in place from the table (idle CTAs see entry 0 and use none of it)
+  const BatchGeom& bg = geoms[active ? bm.geom : 0u];
+  const FftGeom& g = bg.g;
+  const float2* twl = bg.twl;
+  const float2* twc = bg.twc;
   const SampleLoaderOTF ld{in + bm.in_off, bm.n_point, window};
   float2* slot = xch + bm.spec_off;
   if (active && g.C > 1) {

@@ -39,9 +39,10 @@ struct PassQ {
   static constexpr int value = (EPT + R - 1) / R;
 };
 
-// Integer j mod Ns and j - j mod Ns for the runtime stride of a pass.
-SPX_DEV uint32_t mod_ns(uint32_t j, uint32_t Ns) {
-  return ((Ns & (Ns - 1)) == 0) ? (j & (Ns - 1)) : (j % Ns);
+// j mod Ns for the runtime stride of a pass, with magic = ceil(2^32 / Ns)
+// (0 when Ns = 1): exact while j * Ns < 2^32 (j, Ns <= 16384 here).
+SPX_DEV uint32_t mod_ns(uint32_t j, uint32_t Ns, uint32_t magic) {
+  return magic ? j - Ns * __umulhi(j, magic) : 0u;
 }
 
 // Read-only load of a sample that is used once: not allocated in L1, so the
@@ -70,7 +71,7 @@ SPX_DEV float2 load_sample(const float2* __restrict__ x, uint32_t n,
 // One in-place Stockham pass over shared memory.  Loads all of a thread's
 // butterflies, synchronises, computes, stores, synchronises.
 template <int R, int Q>
-SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns,
+SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns, uint32_t magic,
                        const float2* __restrict__ tw, uint32_t tid, uint32_t T) {
   const uint32_t B = M / R;
   float2 v[Q][R];
@@ -87,7 +88,7 @@ SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns,
   for (int q = 0; q < Q; ++q) {
     const uint32_t j = tid + q * T;
     if (j < B) {
-      const uint32_t k = mod_ns(j, Ns);
+      const uint32_t k = mod_ns(j, Ns, magic);
       if (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(tw + (r - 1) * Ns + k));
@@ -228,7 +229,7 @@ template <int R, int EPT>
 SPX_DEV uint32_t run_radix(float2* s, const FftGeom& g, uint32_t p,
                            const float2* __restrict__ tw_local, uint32_t tid, uint32_t T) {
   while (p < g.npass && g.radix[p] == R) {
-    pass_smem<R, PassQ<EPT, R>::value>(s, g.M, g.ns[p], tw_local + g.twoff[p], tid, T);
+    pass_smem<R, PassQ<EPT, R>::value>(s, g.M, g.ns[p], g.nsmagic[p], tw_local + g.twoff[p], tid, T);
     ++p;
   }
   return p;

@@ -124,6 +124,7 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept, uint32_t pref_local) {
     r.radix[p] = rad[p];
     r.ns[p] = Ns;
     r.twoff[p] = off;
+    r.nsmagic[p] = Ns > 1 ? (uint32_t)(((1ull << 32) + Ns - 1) / Ns) : 0u;
     off += Ns * (rad[p] - 1);
     Ns *= rad[p];
   }

@@ -24,6 +24,7 @@ struct FftGeom {
   uint32_t radix[kMaxPass];
   uint32_t ns[kMaxPass];
   uint32_t twoff[kMaxPass];
+  uint32_t nsmagic[kMaxPass];  // ceil(2^32 / ns[p]) (0 for ns = 1): j mod ns = j - ns * umulhi(j, magic)
   // Set per launch (0 in plans): beams in the launch and the L2 prefetch
   // distance in beams (the beams resident at once; 0 = no prefetch).
   uint32_t beams;
