@@ -38,7 +38,7 @@ SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
 # DRAM bytes (read + write) of one fft_peaks_kernel launch on this workload,
 # from an ncu capture (profiles/fft_peaks_kernel_plain_large.md).
-NCU_TRAFFIC_BYTES = 145_510_912
+NCU_TRAFFIC_BYTES = 143_483_392
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
