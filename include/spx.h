@@ -257,10 +257,11 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
  * 117-119; src/fft_func/src/spectrum_processor_rocm.cpp:444-500).  h_in holds
  * beams x n_point complex64; h_out receives beams x R MaxValue (R = 4 ONE,
  * 8 TWO, the spx_all_maxima_capacity for ALL, K for TOPK) and h_counts the
- * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO).  The beams go through
- * in ~16 MiB chunks whose upload, transform and read-back overlap on three
- * streams; page-locked host buffers (cudaHostAlloc / cudaHostRegister) are
- * needed for the overlap.  Returns after the results are in host memory. */
+ * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO).  Page-locked,
+ * device-mapped input (cudaHostAlloc; cudaHostRegister with mapping) is read
+ * by the kernel in place over the host link; other input goes through in
+ * ~16 MiB chunks whose upload, transform and read-back overlap on three
+ * streams.  Returns after the results are in host memory. */
 spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
                               uint32_t n_point, uint32_t nfft, uint32_t window,
                               const spx_peak_params* params, spx_max_value* h_out,

@@ -136,7 +136,7 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   float2* scratch = static_cast<float2*>(scr);
   dim3 grid(kBigM / 32, beams);
   const void* kcols = g.C == 64 ? (const void*)big_cols_kernel<64> : (const void*)big_cols_kernel<32>;
-  const uint32_t ahead_cols = resident_ctas(kcols, 256, 0, 1);
+  const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, 256, 0, 1);
   if (g.C == 64)
     big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
                                                        ahead_cols);

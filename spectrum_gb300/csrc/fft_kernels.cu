@@ -310,11 +310,11 @@ uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem) {
 
 template <typename K>
 static cudaError_t launch_beams(K kernel, FftGeom& g, uint32_t beams, size_t smem,
-                                cudaStream_t stream, void** args) {
+                                cudaStream_t stream, void** args, bool prefetch) {
   cudaError_t e0 = configure_kernel((const void*)kernel, kMaxLocal * sizeof(float2) + 16384);
   if (e0 != cudaSuccess) return e0;
   g.beams = beams;
-  g.ahead = resident_beams((const void*)kernel, g, smem);
+  g.ahead = prefetch ? resident_beams((const void*)kernel, g, smem) : 0u;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(beams * g.C, 1, 1);
   cfg.blockDim = dim3(g.T, 1, 1);
@@ -347,8 +347,8 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
                     (void*)&twl,  (void*)&twc,     (void*)&d_out, (void*)&out_mode,
                     (void*)&scale};
-    e = wide ? launch_beams(fft_out_kernel<32>, g, beams, smem, ctx->stream, args)
-             : launch_beams(fft_out_kernel<16>, g, beams, smem, ctx->stream, args);
+    e = wide ? launch_beams(fft_out_kernel<32>, g, beams, smem, ctx->stream, args, !ctx->input_on_host)
+             : launch_beams(fft_out_kernel<16>, g, beams, smem, ctx->stream, args, !ctx->input_on_host);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
     return SPX_OK;
   }
@@ -358,8 +358,8 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   float2* xchp = static_cast<float2*>(xch);
   void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
                   (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};
-  e = wide ? launch_beams(fft_xl_kernel<32>, g, beams, smem, ctx->stream, args)
-           : launch_beams(fft_xl_kernel<16>, g, beams, smem, ctx->stream, args);
+  e = wide ? launch_beams(fft_xl_kernel<32>, g, beams, smem, ctx->stream, args, !ctx->input_on_host)
+           : launch_beams(fft_xl_kernel<16>, g, beams, smem, ctx->stream, args, !ctx->input_on_host);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_xl_kernel");
   return SPX_OK;
 }

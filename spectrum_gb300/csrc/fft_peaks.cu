@@ -478,7 +478,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   e = configure_kernel(kfn, 227 * 1024);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
   g.beams = beams;
-  g.ahead = resident_beams(kfn, g, smem);
+  g.ahead = ctx->input_on_host ? 0u : resident_beams(kfn, g, smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(beams * g.C, 1, 1);
   cfg.blockDim = dim3(g.T, 1, 1);

@@ -3,16 +3,21 @@
 // FindAllMaximaFromCPU (src/fft_func/src/spectrum_processor_rocm.cpp:444-500:
 // upload, FFT, peak search, read back).
 //
-// The beams go through in chunks of about kChunkBytes of samples on three
-// streams: copy-in (host -> device), the context's stream (the fused
-// spx_fft_peaks launch) and copy-out (device -> host), so the upload of chunk
+// Page-locked input that the device can address (cudaHostAlloc, or
+// cudaHostRegister with mapping) is read by the kernel in place over the
+// host link; the peaks are written in place too when the output buffers are
+// mapped, else they come back in one copy.  Other input goes through in
+// chunks of about kChunkBytes of samples on three streams: copy-in (host ->
+// device), the context's stream (the fused spx_fft_peaks launch) and
+// copy-out (device -> host), so the upload of chunk
 // i + 1 overlaps the transform of chunk i and the read-back of chunk i - 1.
 // Staging: three input slots and two output slots in one device buffer owned
 // by the context.  Events order slot reuse:
 //   copy-in of chunk i waits until chunk i - 3 was computed (its input slot);
 //   compute of chunk i waits for its upload and for the read-back of chunk
 //   i - 2 (its output slot).
-// With pageable host memory the copies are still correct but do not overlap.
+// With pageable host memory the chunk copies are still correct but do not
+// overlap.
 #include <algorithm>
 #include <cstring>
 
@@ -78,6 +83,46 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
     default: per = params->max_per_beam; break;
   }
   DeviceGuard guard(ctx->device);
+  // Page-locked, device-mapped input: the kernel reads it over the host link
+  // itself (the link carries ~210 GB/s either way; reading in place has no
+  // pipeline fill or drain), results come back in one copy.
+  auto device_view = [](const void* p) -> void* {
+    cudaPointerAttributes a{};
+    const bool ok = p && cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    return ok ? a.devicePointer : nullptr;
+  };
+  cudaPointerAttributes pa{};
+  pa.devicePointer = device_view(h_in);
+  const bool mapped = pa.devicePointer != nullptr;
+  void* dv_out = mapped ? device_view(h_out) : nullptr;
+  void* dv_cnt = mapped && counted ? device_view(h_counts) : nullptr;
+  if (mapped && dv_out && (!counted || dv_cnt)) {  // everything in place
+    ctx->input_on_host = true;
+    spx_status st0 = spx_fft_peaks(ctx, pa.devicePointer, beams, n_point, nfft, window, params,
+                                   static_cast<spx_max_value*>(dv_out), static_cast<uint32_t*>(dv_cnt));
+    ctx->input_on_host = false;
+    if (st0 != SPX_OK) return st0;
+    return spx_synchronize(ctx);
+  }
+  if (mapped) {
+    const size_t out_bytes = align_up((size_t)beams * std::max<uint32_t>(per, 1) * sizeof(spx_max_value), 256);
+    spx_status st0 = ensure_pipeline(ctx, out_bytes + (size_t)beams * sizeof(uint32_t), 0);
+    if (st0 != SPX_OK) return st0;
+    char* o = static_cast<char*>(ctx->d_stage);
+    uint32_t* c = reinterpret_cast<uint32_t*>(o + out_bytes);
+    ctx->input_on_host = true;
+    st0 = spx_fft_peaks(ctx, pa.devicePointer, beams, n_point, nfft, window, params,
+                        reinterpret_cast<spx_max_value*>(o), counted ? c : nullptr);
+    ctx->input_on_host = false;
+    if (st0 != SPX_OK) return st0;
+    cudaError_t e0 = cudaMemcpyAsync(h_out, o, (size_t)beams * per * sizeof(spx_max_value), cudaMemcpyDeviceToHost,
+                                     ctx->stream);
+    if (e0 == cudaSuccess && counted)
+      e0 = cudaMemcpyAsync(h_counts, c, (size_t)beams * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "spx_fft_peaks_host: read-back");
+    return spx_synchronize(ctx);
+  }
   const size_t beam_in = (size_t)n_point * sizeof(float2);
   const uint32_t cb = (uint32_t)std::max<size_t>(1, std::min<size_t>(beams, kChunkBytes / beam_in));
   const uint32_t nchunks = (beams + cb - 1) / cb;

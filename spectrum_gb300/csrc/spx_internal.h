@@ -53,6 +53,8 @@ struct spx_ctx {
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
   std::vector<cudaEvent_t> events;
+  // Set while a launch reads its samples from host memory (no L2 prefetch).
+  bool input_on_host = false;
 };
 
 namespace spx {
