@@ -537,7 +537,7 @@ def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
     return {"value": round(BEAMS * N_POINT / (ms * 1e-3) / 1e6, 2), "unit": "Msamples/s",
             "ms_per_step": round(ms, 4), "h2d_bytes_per_step": int(host_in.numel() * 8),
             "d2h_bytes_per_step": int(host_out.numel() * 4 + host_cnt.numel() * 4),
-            "api": "spx_fft_peaks_host (pinned host buffers, 16 MiB chunks, copy/compute overlap)",
+            "api": "spx_fft_peaks_host (page-locked host buffers read and written in place over the host link)",
             "counts_match_device_path": same}
 
 
