@@ -13,6 +13,8 @@
 //                                             (src/fft_func/src/spectrum_processor_factory.cpp:13-37)
 //   antenna_fft::IAllMaximaPipeline,       <- the same interface
 //   antenna_fft::AllMaximaPipelineGB300       (include/spectrum/interface/i_all_maxima_pipeline.hpp:55-81)
+//   spectrum_utils::GpuFFT                 <- CpuFFT's static API on the GPU
+//                                             (include/spectrum/utils/cpu_fft.hpp:68-203)
 // spectrum_gb300/rocm_names.hpp adds the reference's *ROCm class names as aliases.
 //
 // Errors: std::invalid_argument for bad arguments (null pointers, size
@@ -409,3 +411,22 @@ class SpectrumProcessorFactory {
 };
 
 }  // namespace antenna_fft
+
+// ---------------------------------------------------------------------------
+// CpuFFT's static API (include/spectrum/utils/cpu_fft.hpp:68-203) computed on
+// GPU 0: host vectors in and out, one transform per call.  Lengths must be
+// transform sizes of this build (2^a 3^b up to 262144, 2^19, 2^20):
+// std::invalid_argument otherwise; an empty input throws std::runtime_error
+// as CpuFFT does.
+// ---------------------------------------------------------------------------
+namespace spectrum_utils {
+
+struct GpuFFT {
+  static std::vector<std::complex<float>> ForwardC2C(const std::vector<std::complex<float>>& input);
+  static std::vector<std::complex<float>> InverseC2C(const std::vector<std::complex<float>>& input);
+  static std::vector<std::complex<float>> ForwardR2C(const std::vector<float>& input);
+  static std::vector<std::complex<float>> ForwardR2C_Full(const std::vector<float>& input);
+  static std::vector<float> Magnitude(const std::vector<std::complex<float>>& spectrum, bool squared = false);
+};
+
+}  // namespace spectrum_utils

@@ -187,6 +187,20 @@ spx_status spx_fft(spx_ctx* ctx, const void* d_in, uint32_t beams,
                    uint32_t n_point, uint32_t nfft, uint32_t window,
                    uint32_t out_mode, float scale, void* d_out);
 
+/* Batched inverse C2C FFT with 1/nfft scaling, x[n] = (1/nfft) sum_k X[k]
+ * exp(+2 pi i k n / nfft): the reference's CpuFFT::InverseC2C
+ * (include/spectrum/utils/cpu_fft.hpp:96-118) on the GPU.  d_in / d_out:
+ * complex64 [beams x nfft]; d_out may equal d_in. */
+spx_status spx_ifft(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_t nfft, void* d_out);
+
+/* Batched FFT of real samples (float [beams x n_point]) with window and zero
+ * padding to nfft as spx_fft.  full = 0: nfft/2 + 1 bins per beam
+ * (CpuFFT::ForwardR2C, cpu_fft.hpp:131-152); full = 1: nfft bins, the upper
+ * half the conjugate mirror X[nfft - k] = conj(X[k]) (CpuFFT::ForwardR2C_Full,
+ * cpu_fft.hpp:165-180).  d_out: complex64 [beams x (nfft/2 + 1 or nfft)]. */
+spx_status spx_fft_r2c(spx_ctx* ctx, const float* d_in, uint32_t beams, uint32_t n_point,
+                       uint32_t nfft, uint32_t window, int full, void* d_out);
+
 /* ---- magnitude / phase -------------------------------------------------- */
 /* d_out[i] = |d_in[i]| * inv_n (squared: |d_in[i]|^2 * inv_n), count complex64 elements. */
 spx_status spx_magnitude(spx_ctx* ctx, const void* d_in, float* d_out,

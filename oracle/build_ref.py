@@ -61,11 +61,14 @@ def build(force: bool = False) -> dict:
     pocket = REF / "third_party" / "pocketfft"
     libs = {"cpufft": OUT / "libref_cpufft.so", "kernels": OUT / "libref_kernels.so"}
 
-    if force or not libs["cpufft"].exists():
+    def stale(lib: Path, *srcs: Path) -> bool:
+        return force or not lib.exists() or any(src.stat().st_mtime > lib.stat().st_mtime for src in srcs)
+
+    if stale(libs["cpufft"], HERE / "ref_cpufft_shim.cpp"):
         _run(CXX + ["-shared", "-fPIC", f"-I{inc}", f"-I{pocket}", HERE / "ref_cpufft_shim.cpp",
                     "-o", libs["cpufft"]])
 
-    if force or not libs["kernels"].exists():
+    if stale(libs["kernels"], HERE / "ref_kernels_host.cpp", HERE / "ref_simt.h", HERE / "ref_kernel_dump.cpp"):
         dump = OUT / "ref_kernel_dump"
         _run(CXX + ["-DENABLE_ROCM=1", f"-I{inc}", HERE / "ref_kernel_dump.cpp", "-o", dump])
         raw = [OUT / "spectrum.txt", OUT / "allmax.txt", OUT / "fftproc.txt"]

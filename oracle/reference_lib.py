@@ -34,6 +34,8 @@ def _lib(name):
             lib.ref_pad_windowed.argtypes = [C.c_void_p, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_int]
         else:
             lib.ref_cpu_fft_c2c.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t]
+            lib.ref_cpu_ifft_c2c.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t]
+            lib.ref_cpu_fft_r2c.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_int]
             lib.ref_cpu_magnitude.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
         _libs[name] = lib
     return _libs[name]
@@ -48,6 +50,23 @@ def cpu_fft_c2c(x: np.ndarray) -> np.ndarray:
     x = np.ascontiguousarray(np.atleast_2d(x), np.complex64)
     out = np.empty_like(x)
     _lib("cpufft").ref_cpu_fft_c2c(_p(x), _p(out), x.shape[0], x.shape[1])
+    return out
+
+
+def cpu_ifft_c2c(x: np.ndarray) -> np.ndarray:
+    """CpuFFT::InverseC2C (1/N) row by row."""
+    x = np.ascontiguousarray(np.atleast_2d(x), np.complex64)
+    out = np.empty_like(x)
+    _lib("cpufft").ref_cpu_ifft_c2c(_p(x), _p(out), x.shape[0], x.shape[1])
+    return out
+
+
+def cpu_fft_r2c(x: np.ndarray, full: bool = False) -> np.ndarray:
+    """CpuFFT::ForwardR2C (n/2 + 1 bins) or ForwardR2C_Full (n bins) row by row."""
+    x = np.ascontiguousarray(np.atleast_2d(x), np.float32)
+    n = x.shape[1]
+    out = np.empty((x.shape[0], n if full else n // 2 + 1), np.complex64)
+    _lib("cpufft").ref_cpu_fft_r2c(_p(x), _p(out), x.shape[0], n, 1 if full else 0)
     return out
 
 

@@ -142,6 +142,32 @@ def fft_fp32(x: np.ndarray, nfft: int, win: int = WINDOW_NONE) -> np.ndarray:
     return out
 
 
+def ifft_fp32(X: np.ndarray) -> np.ndarray:
+    """Inverse C2C with 1/N in FP32 (pocketfft via numpy): CpuFFT::InverseC2C
+    (include/spectrum/utils/cpu_fft.hpp:96-118, backward c2c with fct 1/N)."""
+    out = np.fft.ifft(np.atleast_2d(X).astype(np.complex64), axis=-1)
+    assert out.dtype == np.complex64
+    return out
+
+
+def fft_r2c_fp32(x: np.ndarray, nfft: int, win: int = WINDOW_NONE, full: bool = False) -> np.ndarray:
+    """Real-input FFT in FP32: CpuFFT::ForwardR2C (nfft/2 + 1 bins,
+    cpu_fft.hpp:131-152) or ForwardR2C_Full (nfft bins, upper half
+    conj(X[nfft - k]), cpu_fft.hpp:165-180), after window and zero padding."""
+    xr = np.atleast_2d(x).astype(np.float32)
+    w = window(win, xr.shape[-1])
+    if w is not None:
+        xr = (xr * w).astype(np.float32)
+    half = np.fft.rfft(xr, n=nfft, axis=-1).astype(np.complex64)
+    if not full:
+        return half
+    out = np.empty(xr.shape[:-1] + (nfft,), np.complex64)
+    out[..., : half.shape[-1]] = half
+    k = np.arange(half.shape[-1], nfft)
+    out[..., k] = np.conj(half[..., nfft - k])
+    return out
+
+
 def fft_fp64(x: np.ndarray, nfft: int, win: int = WINDOW_NONE) -> np.ndarray:
     """The same transform in FP64 (window in FP64 too): the accuracy reference."""
     x = np.atleast_2d(x).astype(np.complex128)

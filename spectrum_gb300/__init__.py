@@ -6,9 +6,10 @@ binds it with ctypes and offers two layers on top:
 
 * tensor functions (``fft``, ``magnitude``, ``all_maxima`` ...) that take and
   return CUDA ``torch.Tensor`` objects and run on torch's current stream;
-* ``processors``: classes mirroring the reference's Python module
-  ``dsp_spectrum`` (FFTProcessorROCm, SpectrumMaximaFinderROCm,
-  ComplexToMagROCm) for drop-in use.
+* ``spectrum_gb300.dsp_spectrum``: classes mirroring the reference's Python
+  module ``dsp_spectrum`` (FFTProcessorROCm, SpectrumMaximaFinderROCm,
+  ComplexToMagROCm) for drop-in use; ``batch`` (uneven beams) and
+  ``learned`` (learned sub-bin refinement).
 
 PyTorch is used only for device memory and streams.  There is no CPU
 fallback: without the native library and a CUDA device every call raises.
@@ -126,6 +127,33 @@ def fft(x, nfft: int | None = None, window: int = WINDOW_NONE, out: str = "compl
         o = torch.empty(shape, dtype=torch.float32, device=x.device)
     c = _ctx_for(x, ctx)
     c.check(lib.spx_fft(c.h, _ptr(x2), beams, n_point, nfft, window, mode, scale, _ptr(o)))
+    return o
+
+
+def ifft(spec, out=None, ctx: Context | None = None):
+    """Inverse FFT with 1/nfft scaling of spec [beams, nfft] complex64 (CpuFFT::InverseC2C)."""
+    torch = _torch()
+    _require_cuda(spec, torch.complex64, "spec")
+    s2 = spec.reshape(-1, spec.shape[-1])
+    beams, nfft = s2.shape
+    o = torch.empty_like(s2) if out is None else out
+    c = _ctx_for(spec, ctx)
+    c.check(lib.spx_ifft(c.h, _ptr(s2), beams, nfft, _ptr(o)))
+    return o.reshape(spec.shape)
+
+
+def fft_r2c(x, nfft: int | None = None, window: int = WINDOW_NONE, full: bool = False,
+            ctx: Context | None = None):
+    """FFT of real x [beams, n_point] float32 -> complex64 [beams, nfft/2 + 1]
+    (CpuFFT::ForwardR2C) or [beams, nfft] with the conjugate mirror (full)."""
+    torch = _torch()
+    _require_cuda(x, torch.float32, "x")
+    x2 = x.reshape(-1, x.shape[-1])
+    beams, n_point = x2.shape
+    nfft = int(nfft or n_point)
+    o = torch.empty((beams, nfft if full else nfft // 2 + 1), dtype=torch.complex64, device=x.device)
+    c = _ctx_for(x, ctx)
+    c.check(lib.spx_fft_r2c(c.h, _ptr(x2), beams, n_point, nfft, window, 1 if full else 0, _ptr(o)))
     return o
 
 

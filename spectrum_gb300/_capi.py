@@ -81,6 +81,8 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_all_maxima_capacity": (_i, [_u32, _u32, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "spx_noise_threshold_factor": (_f, [_f]),
     "spx_fft": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, _u32, _f, _vp]),
+    "spx_ifft": (_i, [_vp, _vp, _u32, _u32, _vp]),
+    "spx_fft_r2c": (_i, [_vp, _vp, _u32, _u32, _u32, _u32, _i, _vp]),
     "spx_magnitude": (_i, [_vp, _vp, _vp, _u64, _f, _i]),
     "spx_mag_phase": (_i, [_vp, _vp, _vp, _u64]),
     "spx_peaks_one_two": (_i, [_vp, _vp, _u32, _u32, _u32, _f, _i, _vp]),

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <functional>
 #include <stdexcept>
 #include <type_traits>
 
@@ -795,3 +796,78 @@ std::unique_ptr<ISpectrumProcessor> SpectrumProcessorFactory::Create(drv_gpu_lib
 }
 
 }  // namespace antenna_fft
+
+// ===========================================================================
+// spectrum_utils::GpuFFT
+// ===========================================================================
+namespace spectrum_utils {
+
+namespace {
+
+// One context and staging buffers on device 0 for the static API; never
+// destroyed (process-lifetime, like a library singleton).
+struct GpuFFTState {
+  drv_gpu_lib::CudaBackend backend{0, nullptr};
+  spectrum_gb300::Context ctx{&backend};
+  spectrum_gb300::DeviceBuffer in, out;
+};
+
+GpuFFTState& state() {
+  static GpuFFTState* s = new GpuFFTState();
+  return *s;
+}
+
+template <class In, class Out>
+std::vector<Out> run(const std::vector<In>& input, size_t out_len, const char* where,
+                     const std::function<spx_status(spx_ctx*, const void*, void*)>& call) {
+  if (input.empty()) throw std::runtime_error(std::string("GpuFFT::") + where + ": empty input");
+  GpuFFTState& st = state();
+  void* d_in = st.in.ensure(input.size() * sizeof(In), where);
+  void* d_out = st.out.ensure(out_len * sizeof(Out), where);
+  spectrum_gb300::cuda_check(cudaMemcpy(d_in, input.data(), input.size() * sizeof(In), cudaMemcpyHostToDevice), where);
+  st.ctx.check(call(st.ctx.get(), d_in, d_out), where);
+  st.ctx.check(spx_synchronize(st.ctx.get()), where);
+  std::vector<Out> r(out_len);
+  spectrum_gb300::cuda_check(cudaMemcpy(r.data(), d_out, out_len * sizeof(Out), cudaMemcpyDeviceToHost), where);
+  return r;
+}
+
+}  // namespace
+
+std::vector<std::complex<float>> GpuFFT::ForwardC2C(const std::vector<std::complex<float>>& input) {
+  const uint32_t n = (uint32_t)input.size();
+  return run<std::complex<float>, std::complex<float>>(input, n, "ForwardC2C", [n](spx_ctx* c, const void* i, void* o) {
+    return spx_fft(c, i, 1, n, n, SPX_WINDOW_NONE, SPX_OUT_COMPLEX, 1.0f, o);
+  });
+}
+
+std::vector<std::complex<float>> GpuFFT::InverseC2C(const std::vector<std::complex<float>>& input) {
+  const uint32_t n = (uint32_t)input.size();
+  return run<std::complex<float>, std::complex<float>>(input, n, "InverseC2C", [n](spx_ctx* c, const void* i, void* o) {
+    return spx_ifft(c, i, 1, n, o);
+  });
+}
+
+std::vector<std::complex<float>> GpuFFT::ForwardR2C(const std::vector<float>& input) {
+  const uint32_t n = (uint32_t)input.size();
+  return run<float, std::complex<float>>(input, n / 2 + 1, "ForwardR2C", [n](spx_ctx* c, const void* i, void* o) {
+    return spx_fft_r2c(c, static_cast<const float*>(i), 1, n, n, SPX_WINDOW_NONE, 0, o);
+  });
+}
+
+std::vector<std::complex<float>> GpuFFT::ForwardR2C_Full(const std::vector<float>& input) {
+  const uint32_t n = (uint32_t)input.size();
+  return run<float, std::complex<float>>(input, n, "ForwardR2C_Full", [n](spx_ctx* c, const void* i, void* o) {
+    return spx_fft_r2c(c, static_cast<const float*>(i), 1, n, n, SPX_WINDOW_NONE, 1, o);
+  });
+}
+
+std::vector<float> GpuFFT::Magnitude(const std::vector<std::complex<float>>& spectrum, bool squared) {
+  if (spectrum.empty()) return {};
+  const uint64_t n = spectrum.size();
+  return run<std::complex<float>, float>(spectrum, n, "Magnitude", [n, squared](spx_ctx* c, const void* i, void* o) {
+    return spx_magnitude(c, i, static_cast<float*>(o), n, 1.0f, squared ? 1 : 0);
+  });
+}
+
+}  // namespace spectrum_utils

@@ -349,6 +349,11 @@ SPX_DEV void local_fft(float2* s, const FftGeom& g, const Load& load, const floa
   local_passes<EPT>(s, g, 1, tw, tid, T);
 }
 
+// Output modes of the inverse and real-input transforms (beyond spx_fft_out).
+constexpr uint32_t kOutComplexReversed = 16;  // out[(nfft - k) mod nfft] = X[k] * scale
+constexpr uint32_t kOutR2CHalf = 17;          // k <= nfft/2: out[beam (nfft/2 + 1) + k] = X[k]
+constexpr uint32_t kOutR2CFull = 18;          // k <= nfft/2: X[k] at k, conj(X[k]) at nfft - k
+
 // Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
 SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
                           void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
@@ -370,11 +375,41 @@ SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_
       for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag2_rn(s[sw(i)]), scale);
       break;
     }
-    default: {  // SPX_OUT_MAGPHASE
+    case SPX_OUT_MAGPHASE: {
       float2* o = reinterpret_cast<float2*>(out) + obase;
       for (uint32_t i = tid; i < g.M; i += T) {
         float2 z = s[sw(i)];
         o[(size_t)g.C * i] = make_float2(mag_rn(z), atan2f(z.y, z.x));
+      }
+      break;
+    }
+    case kOutComplexReversed: {  // IFFT(X)[n] = FFT(X)[(N - n) mod N] / N
+      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * g.nfft;
+      for (uint32_t i = tid; i < g.M; i += T) {
+        const uint32_t k = c + g.C * i, n = k == 0 ? 0u : g.nfft - k;
+        const float2 z = s[sw(i)];
+        o[n] = make_float2(__fmul_rn(z.x, scale), __fmul_rn(z.y, scale));
+      }
+      break;
+    }
+    case kOutR2CHalf: {
+      const uint32_t half = g.nfft / 2;
+      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * (half + 1);
+      for (uint32_t i = tid; i < g.M; i += T) {
+        const uint32_t k = c + g.C * i;
+        if (k <= half) o[k] = s[sw(i)];
+      }
+      break;
+    }
+    default: {  // kOutR2CFull: the half spectrum and its conjugate mirror
+      const uint32_t half = g.nfft / 2;
+      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * g.nfft;
+      for (uint32_t i = tid; i < g.M; i += T) {
+        const uint32_t k = c + g.C * i;
+        if (k > half) continue;
+        const float2 z = s[sw(i)];
+        o[k] = z;
+        if (k >= 1 && k < g.nfft - half) o[g.nfft - k] = make_float2(z.x, -z.y);
       }
       break;
     }

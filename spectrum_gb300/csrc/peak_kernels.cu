@@ -379,6 +379,20 @@ all_maxima_kernel(AmArgs a) {
   }
 }
 
+// Real samples -> complex samples with zero imaginary part (input of the
+// real-input transform).
+__global__ void widen_real_kernel(const float* __restrict__ in, float2* __restrict__ out, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = make_float2(__ldg(in + i), 0.0f);
+}
+
+spx_status launch_widen_real(spx_ctx* ctx, const float* d_in, float2* d_out, uint64_t n) {
+  const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  widen_real_kernel<<<grid, 256, 0, ctx->stream>>>(d_in, d_out, n);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch widen_real_kernel");
+}
+
 // Self-test of the bounded wait: one thread waits, as tile 1 of a beam, on
 // tile 0's status word, which holds another epoch and is never published, so
 // the wait ends at its time bound and sets kErrLookbackTimeout.

@@ -7,6 +7,7 @@
 #include <new>
 #include <string>
 
+#include "fft_core.cuh"
 #include "spx_internal.h"
 
 namespace spx {
@@ -270,6 +271,44 @@ spx_status spx_fft(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_t n_po
   if (st != SPX_OK) return st;
   return launch_fft_out(ctx, *plan, static_cast<const float2*>(d_in), beams, n_point, win,
                         out_mode, scale, d_out);
+}
+
+spx_status spx_ifft(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_t nfft, void* d_out) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (beams == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_ifft: null device pointer");
+  if (nfft == 0) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_ifft: nfft must be > 0");
+  DeviceGuard g(ctx->device);
+  const FftPlan* plan = nullptr;
+  spx_status st = get_plan(ctx, nfft, &plan);
+  if (st != SPX_OK) return st;
+  // x[n] = FFT(X)[(nfft - n) mod nfft] / nfft: the forward transform with a
+  // reversing, scaling epilogue
+  return launch_fft_out(ctx, *plan, static_cast<const float2*>(d_in), beams, nfft, nullptr,
+                        kOutComplexReversed, 1.0f / (float)nfft, d_out);
+}
+
+spx_status spx_fft_r2c(spx_ctx* ctx, const float* d_in, uint32_t beams, uint32_t n_point,
+                       uint32_t nfft, uint32_t window, int full, void* d_out) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  if (beams == 0) return SPX_OK;
+  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_r2c: null device pointer");
+  if (n_point == 0 || nfft < n_point)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_r2c: need 0 < n_point <= nfft");
+  DeviceGuard g(ctx->device);
+  const FftPlan* plan = nullptr;
+  spx_status st = get_plan(ctx, nfft, &plan);
+  if (st != SPX_OK) return st;
+  const float* win = nullptr;
+  st = get_window(ctx, window, n_point, &win);
+  if (st != SPX_OK) return st;
+  void* wide = nullptr;
+  st = get_scratch(ctx, kSlotSpectrum, (size_t)beams * n_point * sizeof(float2), &wide);
+  if (st != SPX_OK) return st;
+  st = launch_widen_real(ctx, d_in, static_cast<float2*>(wide), (uint64_t)beams * n_point);
+  if (st != SPX_OK) return st;
+  return launch_fft_out(ctx, *plan, static_cast<const float2*>(wide), beams, n_point, win,
+                        full ? kOutR2CFull : kOutR2CHalf, 1.0f, d_out);
 }
 
 spx_status spx_magnitude(spx_ctx* ctx, const void* d_in, float* d_out, uint64_t count,

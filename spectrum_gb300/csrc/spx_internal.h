@@ -130,6 +130,8 @@ spx_status launch_topk(spx_ctx* ctx, const float* d_mag, const float2* d_fft,
 // the L2 prefetch distance of the FFT kernels.
 uint32_t resident_ctas(const void* kernel, uint32_t threads, size_t smem, uint32_t cluster);
 uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem);
+// Real samples widened to complex (imaginary part 0).
+spx_status launch_widen_real(spx_ctx* ctx, const float* d_in, float2* d_out, uint64_t n);
 // Launches one bounded look-back wait that cannot be satisfied (self-test of
 // the timeout path); d_status: 2 words of scratch.
 spx_status launch_lookback_timeout_probe(spx_ctx* ctx, unsigned long long* d_status);

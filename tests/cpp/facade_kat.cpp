@@ -369,6 +369,43 @@ static void spectrum_tests(CudaBackend& be) {
                                       [&] { SpectrumProcessorFactory::Create(BackendType::ROCm, nullptr); });
 }
 
+static void gpufft_tests() {
+  using spectrum_utils::GpuFFT;
+  // forward against a direct DFT (n = 96), inverse round trip, R2C half / full
+  const uint32_t n = 96;
+  std::vector<std::complex<float>> x(n);
+  std::vector<float> r(n);
+  for (uint32_t t = 0; t < n; ++t) {
+    x[t] = {std::cos(0.3f * t) + 0.1f * t / n, std::sin(0.7f * t)};
+    r[t] = std::cos(0.25f * t) - 0.5f * std::sin(0.9f * t);
+  }
+  auto X = GpuFFT::ForwardC2C(x);
+  double err = 0.0, peak = 0.0;
+  for (uint32_t k = 0; k < n; ++k) {
+    std::complex<double> acc = 0.0;
+    for (uint32_t t = 0; t < n; ++t) acc += std::complex<double>(x[t]) * std::polar(1.0, -2.0 * M_PI * k * t / n);
+    err = std::max(err, std::abs(acc - std::complex<double>(X[k])));
+    peak = std::max(peak, std::abs(acc));
+  }
+  check(X.size() == n && err / peak < 1e-5, "gpufft.forward_c2c_vs_dft", std::to_string(err / peak));
+  auto back = GpuFFT::InverseC2C(X);
+  double rt = 0.0;
+  for (uint32_t t = 0; t < n; ++t) rt = std::max(rt, (double)std::abs(back[t] - x[t]));
+  check(rt < 1e-5, "gpufft.inverse_round_trip", std::to_string(rt));
+  auto half = GpuFFT::ForwardR2C(r);
+  auto full = GpuFFT::ForwardR2C_Full(r);
+  bool mirror = half.size() == n / 2 + 1 && full.size() == n;
+  for (uint32_t k = 0; mirror && k <= n / 2; ++k) mirror = full[k] == half[k];
+  for (uint32_t k = n / 2 + 1; mirror && k < n; ++k) mirror = full[k] == std::conj(full[n - k]);
+  check(mirror, "gpufft.r2c_half_and_full_mirror");
+  auto m = GpuFFT::Magnitude({{3.f, 4.f}, {0.f, 0.f}}, false);
+  auto m2 = GpuFFT::Magnitude({{3.f, 4.f}}, true);
+  check(m.size() == 2 && m[0] == 5.f && m[1] == 0.f && m2[0] == 25.f, "gpufft.magnitude");
+  expect_throw<std::runtime_error>("gpufft.empty", [] { GpuFFT::ForwardC2C({}); });
+  expect_throw<std::invalid_argument>("gpufft.unsupported_length",
+                                      [] { GpuFFT::ForwardC2C(std::vector<std::complex<float>>(1000)); });
+}
+
 int main(int argc, char** argv) {
   const bool no_gpu = argc > 1 && std::strcmp(argv[1], "--no-gpu") == 0;
   if (no_gpu) {
@@ -386,6 +423,7 @@ int main(int argc, char** argv) {
       fft_tests(be);
       mag_tests(be);
       spectrum_tests(be);
+      gpufft_tests();
     } catch (const std::exception& e) {
       check(false, "unexpected exception", e.what());
     }

@@ -84,6 +84,16 @@ def main():
     out["kat100_X"] = X
     out["kat100_out"] = ref.post_peaks(X[None], 1024, 0, 10000.0, False).view(np.uint32)
 
+    # 6. CpuFFT::InverseC2C, ForwardR2C, ForwardR2C_Full
+    for n in (64, 1000, 4096):
+        x = _spec(rng, 2, n, False)
+        out[f"ifft{n}_X"] = x
+        out[f"ifft{n}_x"] = ref.cpu_ifft_c2c(x)
+        r = rng.standard_normal((2, n)).astype(np.float32)
+        out[f"r2c{n}_x"] = r
+        out[f"r2c{n}_half"] = ref.cpu_fft_r2c(r, False)
+        out[f"r2c{n}_full"] = ref.cpu_fft_r2c(r, True)
+
     np.savez_compressed(HERE / "reference_golden.npz", **out)
     print(f"wrote {HERE / 'reference_golden.npz'} ({(HERE / 'reference_golden.npz').stat().st_size} bytes)")
 

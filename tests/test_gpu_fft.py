@@ -121,3 +121,66 @@ def test_precision_workload_dynamic_range(spx, cuda):
         weak_mag = np.abs(got[b, weak - 2:weak + 3]).max()
         assert 20 * np.log10(peak / rms) > 150          # dynamic range vs the FP32 error floor
         assert 20 * np.log10(weak_mag / rms) > 40       # the -120 dB tone is visible
+
+
+# ---- inverse and real-input transforms (CpuFFT::InverseC2C / ForwardR2C / ForwardR2C_Full) ----
+
+def _golden():
+    from pathlib import Path
+    return np.load(Path(__file__).parent / "golden" / "reference_golden.npz")
+
+
+@pytest.mark.parametrize("n", [64, 1000, 4096])
+def test_ifft_and_r2c_match_reference_cpufft(spx, cuda, n):
+    """Against the reference's own CpuFFT outputs (golden): 1e-5 of the peak.
+    CpuFFT takes any length; the GPU transforms take 2^a 3^b lengths and
+    reject others (1000 = 2^3 5^3) with SPX_ERR_INVALID_ARG."""
+    import torch
+    G = _golden()
+    if not spx.fft_size_supported(n):
+        with pytest.raises(ValueError):
+            spx.ifft(torch.from_numpy(G[f"ifft{n}_X"]).to(cuda))
+        with pytest.raises(ValueError):
+            spx.fft_r2c(torch.from_numpy(G[f"r2c{n}_x"]).to(cuda))
+        return
+    X, x = G[f"ifft{n}_X"], G[f"ifft{n}_x"]
+    got = spx.ifft(torch.from_numpy(X).to(cuda)).cpu().numpy()
+    assert np.abs(got - x).max() / np.abs(x).max() < FFT_TOL
+    r, half, full = G[f"r2c{n}_x"], G[f"r2c{n}_half"], G[f"r2c{n}_full"]
+    rd = torch.from_numpy(r).to(cuda)
+    gh = spx.fft_r2c(rd).cpu().numpy()
+    gf = spx.fft_r2c(rd, full=True).cpu().numpy()
+    assert gh.shape == half.shape and gf.shape == full.shape
+    assert np.abs(gh - half).max() / np.abs(half).max() < FFT_TOL
+    assert np.abs(gf - full).max() / np.abs(full).max() < FFT_TOL
+    k = np.arange(n // 2 + 1, n)  # the mirror is exact, as in the reference
+    np.testing.assert_array_equal(gf[:, k], np.conj(gf[:, n - k]))
+    np.testing.assert_array_equal(gf[:, : n // 2 + 1], gh)
+
+
+@pytest.mark.parametrize("nfft", [2, 9, 96, 4096, 13122, 65536, 131072, 1 << 20])
+def test_ifft_round_trip_and_fp64(spx, cuda, nfft):
+    import torch
+    beams = 2 if nfft < (1 << 20) else 1
+    x = _signal(beams, nfft, nfft)
+    xd = torch.from_numpy(x).to(cuda)
+    back = spx.ifft(spx.fft(xd)).cpu().numpy()
+    assert np.abs(back - x).max() / np.abs(x).max() < 3e-6
+    got = spx.ifft(xd).cpu().numpy()
+    ref = np.fft.ifft(x.astype(np.complex128), axis=-1)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < FFT_TOL
+    inplace = xd.clone()
+    spx.ifft(inplace, out=inplace)
+    np.testing.assert_array_equal(inplace.cpu().numpy(), got)
+
+
+@pytest.mark.parametrize("n_point,nfft,win,full", [(1000, 1024, 1, False), (6000, 6561, 4, True),
+                                                   (30000, 32768, 2, False), (2187, 2187, 0, True)])
+def test_r2c_window_and_padding(spx, cuda, n_point, nfft, win, full):
+    import torch
+    if not spx.fft_size_supported(nfft):
+        pytest.skip("size")
+    r = np.random.default_rng(n_point).standard_normal((3, n_point)).astype(np.float32)
+    got = spx.fft_r2c(torch.from_numpy(r).to(cuda), nfft, window=win, full=full).cpu().numpy()
+    ref = orc.fft_r2c_fp32(r, nfft, win, full)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < FFT_TOL

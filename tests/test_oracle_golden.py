@@ -71,6 +71,21 @@ def test_fft_matches_reference_cpufft(n):
     assert err < 1e-6, err
 
 
+@pytest.mark.parametrize("n", [64, 1000, 4096])
+def test_inverse_and_real_ffts_match_reference_cpufft(n):
+    """CpuFFT::InverseC2C / ForwardR2C / ForwardR2C_Full of the reference
+    (golden) against the oracle's restatement."""
+    X, x = G[f"ifft{n}_X"], G[f"ifft{n}_x"]
+    assert np.abs(orc.ifft_fp32(X) - x).max() / np.abs(x).max() < 1e-6
+    r, half, full = G[f"r2c{n}_x"], G[f"r2c{n}_half"], G[f"r2c{n}_full"]
+    assert half.shape == (2, n // 2 + 1) and full.shape == (2, n)
+    assert np.abs(orc.fft_r2c_fp32(r, n) - half).max() / np.abs(half).max() < 1e-6
+    got_full = orc.fft_r2c_fp32(r, n, full=True)
+    assert np.abs(got_full - full).max() / np.abs(full).max() < 1e-6
+    k = np.arange(n // 2 + 1, n)   # the reference's mirror is exact
+    np.testing.assert_array_equal(full[:, k], np.conj(full[:, n - k]))
+
+
 def test_known_answer_100hz():
     """tests/test_spectrum_maxima_rocm.hpp:98-126: 100 Hz, fs 10 kHz, 1000 pts -> |f - 100| < 5 Hz."""
     ref = _mv(G["kat100_out"]).reshape(-1)
