@@ -53,13 +53,63 @@ def _parse():
                     help="skip the small / uneven / precision / learned workload timings")
     ap.add_argument("--profile", action="store_true",
                     help="device steps only (warmup + steps), no timing report; for ncu captures")
+    ap.add_argument("--profile-workload", default="large", choices=["large", "plain4096", "plain16384", "uneven"],
+                    help="with --profile: the fused large step, the plain FFT (|X|^2 out) of 16384 x 4096 or "
+                         "2048 x 16384 points, or the uneven batch")
     return ap.parse_args()
+
+
+def run_profile_other(args):
+    """--profile steps of the plain FFT or the uneven batch (for ncu)."""
+    import ctypes as C
+
+    import torch
+
+    import spectrum_gb300 as spx
+    from spectrum_gb300 import synth
+    dev = torch.device("cuda", 0)
+    ctx = spx.default_context(0)
+    ctx.bind_stream()
+    if args.profile_workload == "uneven":
+        from spectrum_gb300.batch import Batch
+        bs = synth.workload_uneven(seed=2)
+        x = synth.synth_torch(bs, device=dev, packed=True)
+        b = Batch(bs.lengths, window=spx.WINDOW_HANN, k=8, sample_rate=1.0, ctx=ctx)
+        for _ in range(args.warmup + args.steps):
+            b.run(x)
+    else:
+        n = 4096 if args.profile_workload == "plain4096" else 16384
+        beams = (1 << 26) // n
+        x = torch.randn(beams, n, dtype=torch.complex64, device=dev)
+        o = torch.empty(beams, n, dtype=torch.float32, device=dev)
+        for _ in range(args.warmup + args.steps):
+            ctx.check(spx.lib.spx_fft(ctx.h, C.c_void_p(x.data_ptr()), beams, n, n, spx.WINDOW_HANN,
+                                      spx.OUT_MAG2, 1.0, C.c_void_p(o.data_ptr())))
+    torch.cuda.synchronize()
 
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     return ws, rank
+
+
+def max_over_ranks(ms: float, device=None) -> float:
+    """The slowest rank's step time (every rank gets it); the local value
+    when no process group is up."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world_size: int, ms: float) -> float:
+    """Whole-job Msamples/s: every rank is a replica processing BEAMS x N_POINT
+    samples per step (weak scaling), timed by the slowest rank."""
+    return world_size * BEAMS * N_POINT / (ms * 1e-3) / 1e6
 
 
 # ---------------------------------------------------------------------------
@@ -250,12 +300,8 @@ def run_gpu(args):
     barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
     clk = clocks.stop()
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * BEAMS * N_POINT / (ms * 1e-3) / 1e6
+    ms = max_over_ranks(ms, dev)
+    value = job_throughput(ws, ms)
 
     # ---- per-kernel timing of the dominant kernel (CUDA events, same stream) ----
     kern = time_components(spx, ctx, xs, out, counts, p, stream, args.steps)
@@ -543,7 +589,9 @@ def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
 
 def main():
     args = _parse()
-    if args.impl == "reference":
+    if args.profile and args.profile_workload != "large":
+        run_profile_other(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
