@@ -105,7 +105,7 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
   std::vector<float2> twl(kBigM);
   for (uint32_t p = 0; p < gl.npass; ++p) {
     const uint32_t R = gl.radix[p], Ns = gl.ns[p];
-    for (uint32_t r = 1; r < R; ++r)
+    for (uint32_t r = 1; r <= tw_rows(R); ++r)
       for (uint32_t k = 0; k < Ns; ++k) {
         const uint64_t L = (uint64_t)Ns * R, m = ((uint64_t)r * k) % L;
         const double a = -2.0 * M_PI * (double)m / (double)L;

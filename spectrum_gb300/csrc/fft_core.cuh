@@ -19,8 +19,8 @@
 // Shared memory layout: element i at sw(i) (spx_device.cuh), length
 // padded to a multiple of 16.  Twiddles are FP32 values of FP64-generated
 // exponentials: tw_local holds, per pass p with radix R and stride Ns,
-// W_{Ns R}^{r k} at [(r-1)*Ns + k]; tw_cross holds W_N^{n2 k1} at
-// [(k1-1)*M + n2].
+// W_{Ns R}^{r k} at [(r-1)*Ns + k] for r <= tw_rows(R) (radix 4: r = 1 only);
+// tw_cross holds W_N^{n2 k1} at [(k1-1)*M + n2].
 #pragma once
 
 #include <cooperative_groups.h>
@@ -90,8 +90,13 @@ SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns, uint32_t magic,
     if (j < B) {
       const uint32_t k = mod_ns(j, Ns, magic);
       if (Ns > 1) {
+        if constexpr (R == 4) {
+          const float2 w1 = __ldg(tw + k), w2 = cmul(w1, w1);
+          v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
+        } else {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(tw + (r - 1) * Ns + k));
+          for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(tw + (r - 1) * Ns + k));
+        }
       }
       Dft<R>::run(v[q]);
       const uint32_t base = (j - k) * R + k;
@@ -269,7 +274,7 @@ constexpr int p2_radix(int p) {
 template <int M>
 constexpr int p2_ns(int p) { return p == 0 ? 1 : p2_ns<M>(p - 1) * p2_radix<M>(p - 1); }
 template <int M>
-constexpr int p2_twoff(int p) { return p == 0 ? 0 : p2_twoff<M>(p - 1) + p2_ns<M>(p - 1) * (p2_radix<M>(p - 1) - 1); }
+constexpr int p2_twoff(int p) { return p == 0 ? 0 : p2_twoff<M>(p - 1) + p2_ns<M>(p - 1) * (p2_radix<M>(p - 1) == 4 ? 1 : p2_radix<M>(p - 1) - 1); }
 
 // First pass (Ns = 1) from device memory, M and the thread count T = M / 16 constant.
 template <int M, typename Load>
@@ -308,8 +313,13 @@ SPX_DEV void p2_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
     const uint32_t j = tid + q * T;
     const uint32_t k = j & (Ns - 1);
     const float2* t = tw + p2_twoff<M>(P) + k;
+    if constexpr (R == 4) {
+      const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
+      v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
+    } else {
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+      for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+    }
     Dft<R>::run(v[q]);
     const uint32_t base = (j - k) * R + k;
     const uint32_t sb = sw(base);

@@ -125,7 +125,7 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept, uint32_t pref_local) {
     r.ns[p] = Ns;
     r.twoff[p] = off;
     r.nsmagic[p] = Ns > 1 ? (uint32_t)(((1ull << 32) + Ns - 1) / Ns) : 0u;
-    off += Ns * (rad[p] - 1);
+    off += Ns * tw_rows(rad[p]);
     Ns *= rad[p];
   }
   uint32_t T = (r.M + ept - 1) / ept;
@@ -175,7 +175,7 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
   std::vector<float2> twl(std::max<uint32_t>(g.M, 1));
   for (uint32_t p = 0; p < g.npass; ++p) {
     const uint32_t R = g.radix[p], Ns = g.ns[p];
-    for (uint32_t r = 1; r < R; ++r)
+    for (uint32_t r = 1; r <= tw_rows(R); ++r)
       for (uint32_t k = 0; k < Ns; ++k)
         twl[g.twoff[p] + (r - 1) * Ns + k] = twiddle((uint64_t)r * k, (uint64_t)Ns * R);
   }

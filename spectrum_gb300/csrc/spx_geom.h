@@ -13,6 +13,12 @@ constexpr int kEPTDefault = 16;         // points held per thread per pass (16 o
 // nfft = C * M.  The M-point local FFT runs npass Stockham passes; pass p
 // has radix radix[p], input stride ns[p] (product of earlier radices) and
 // its twiddles at tw_local + twoff[p].
+// Twiddle rows stored per Stockham pass of radix R: W^{rk}, r = 1..R-1,
+// except radix 4, which stores W^k only and forms W^2k = (W^k)^2 and
+// W^3k = W^2k W^k in the pass: the last pass of a 16384-point FFT reads a
+// 32 KB table instead of 96 KB, which keeps it in L1 beside the window.
+constexpr uint32_t tw_rows(uint32_t R) { return R == 4 ? 1u : R - 1u; }
+
 struct FftGeom {
   uint32_t nfft;
   uint32_t C;       // CTAs per beam (cluster size)
