@@ -1,5 +1,6 @@
 // fft_peaks.cu — fused window + zero pad + FFT + |X| + noise threshold +
-// peak search: the spectrum of a beam never leaves the chip.
+// peak search from raw samples.  nfft <= 16384: one CTA per beam, the
+// spectrum never leaves the chip; larger: see "C > 1" below.
 //
 // Replaces, for one beam per CTA (nfft <= 16384) or per cluster of C CTAs:
 //   PadDataOp + hipfftExecC2C + ComputeMagnitudesOp + AllMaximaPipelineROCm
@@ -8,21 +9,24 @@
 // with the noise threshold and parabolic refinement of this build.
 //
 // Modes:
-//   ALL  + threshold : every strict local maximum of |X| in [start, end) above
-//                      the per-beam threshold, compacted in bin order.
+//   ALL              : every strict local maximum of |X| in [start, end)
+//                      (above the per-beam threshold when one is given),
+//                      compacted in bin order.
 //   TOPK (C == 1)    : the K largest strict local maxima (optionally above the
 //                      threshold), |X| descending, ties by lower bin.
 // Results are bit-identical to spx_fft (COMPLEX) followed by spx_all_maxima /
 // spx_topk: the same FFT code, |X| = sqrt_rn(re*re + im*im), the same
 // histogram-median threshold and the same comparisons.
 //
-// C > 1 (the beam's bins k = c + C*i are spread over the cluster): after the
-// cluster barrier that completes the beam's noise histogram every spectrum is
-// final, so each CTA tests its bins above the threshold (few) against both
-// neighbours read from the neighbours' CTAs (distributed shared memory) and
-// keeps their magnitudes for the refinement; maxima bitmaps go through
-// device memory, and after one more barrier every CTA ranks its maxima by a
-// prefix popcount over the beam's maxima bitmap in bin order.
+// C > 1 (the beam's bins k = c + C*i are spread over the cluster): the
+// cluster FFT writes the bins of the search window into its exchange slot in
+// row layout (row c holds X[c + C*i]; the slot's rows are dead by then) and
+// maxima_cluster_kernel, one small cluster per beam and several clusters per
+// SM, loads |X| of contiguous bin ranges into shared memory, merges their
+// noise histograms through distributed shared memory, and classifies and
+// ranks the maxima.  Two launches instead of one: the per-beam threshold is a
+// dependency across the whole beam, and resolving it inside the FFT cluster
+// (one CTA per SM) left the SMs idle on barriers for ~40 % of the launch.
 #include <cuda/atomic>
 
 #include "fft_core.cuh"
@@ -31,16 +35,13 @@
 namespace spx {
 
 constexpr uint32_t kHist = 4096;  // noise-histogram buckets (exponent + 4 mantissa bits)
-constexpr uint32_t kList = 1024;  // hot bins classified per round (C > 1); >= threads per CTA
 
 struct FusedArgs {
   const float2* in;
   const float* win;
   const float2* tw_local;
   const float2* tw_cross;
-  float2* xch;              // exchange slots (C > 1), one per beam
-  uint32_t* ghist;          // [beams][4096] per-beam histograms (C > 1), zeroed by the host
-  uint32_t* gbits;          // [beams][nfft/32 + C] maxima bitmaps (C > 1)
+  float2* xch;              // exchange slots (C > 1), one per beam; then the window's bins
   MaxValueDev* out;
   uint32_t* counts;
   uint32_t n_point, start, end, cap, mode, K, refine;
@@ -207,189 +208,66 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
 }
 
 // ---------------------------------------------------------------------------
-// C > 1: bins k = c + C*i; see the file comment.
+// C > 1: the cluster FFT writes the bins of the search window (row layout),
+// then maxima_cluster_kernel finds the maxima of each beam.
 // ---------------------------------------------------------------------------
-// Exclusive block-wide prefix of one value per thread; returns the prefix and
-// writes the total to *total (all threads).  Uses s_red[0..65].
-SPX_DEV uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_red, uint32_t* total) {
-  const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  uint32_t x = v;
+// One window of a merged histogram, h[0, W) = buckets b0 .. b0 + W - 1,
+// `below` bins lying in lower buckets; r = (n - 1) / 2 is the median rank.
+// Computed by one warp (every warp of a CTA may call it; no barrier).  If
+// the window holds rank r, *thr = the histogram-interpolated median times
+// `factor` (the arithmetic of threshold_from_hist) and returns true;
+// *total = the window's bins.
+SPX_DEV bool warp_median_window(const uint32_t* h, uint32_t W, uint32_t b0, uint32_t below,
+                                uint32_t r, float factor, float* thr, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t per = (W + 31) / 32;
+  const uint32_t lo = min(lane * per, W), hi = min(lo + per, W);
+  uint32_t sum = 0;
+  for (uint32_t j = lo; j < hi; ++j) sum += h[j];
+  uint32_t x = sum;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= (uint32_t)o) x += y;
   }
-  if (lane == 31) s_red[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    const uint32_t nw = T >> 5;
-    uint32_t w = lane < nw ? s_red[lane] : 0u, u = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
-      if (lane >= (uint32_t)o) u += y;
-    }
-    if (lane < nw) s_red[32 + lane] = u - w;
-    if (lane == nw - 1) s_red[64] = u;
-  }
-  __syncthreads();
-  const uint32_t r = s_red[32 + warp] + x - v;
-  *total = s_red[64];
-  __syncthreads();
-  return r;
-}
-
-SPX_DEV void peaks_cluster(float2* s, uint32_t* shist, uint32_t* s_red, uint32_t* shot,
-                           uint32_t* slist, uint32_t list_cap, const FftGeom& g, uint32_t c,
-                           uint32_t beam, const FusedArgs& a) {
-  cg::cluster_group cl = cg::this_cluster();
-  const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31;
-  const uint32_t C = g.C, M = g.M;
-  const uint32_t n = a.end > a.start ? a.end - a.start : 0;
-  const uint32_t i_start = a.start <= c ? 0u : (a.start - c + C - 1) / C;
-  const uint32_t i_end = a.end <= c ? 0u : min(M, (a.end - c + C - 1) / C);  // first i with k >= end
-  // 1. histogram over [start, end): shared atomics, one global atomic per used bucket.
-  //    After the barrier every CTA's spectrum is final, so DSMEM reads are safe
-  //    until the last barrier below.
-  uint32_t* gh = a.ghist + (size_t)beam * kHist;
-  for (uint32_t i = i_start + tid; i < i_end; i += T) atomicAdd(&shist[bucket_of(mag_rn(s[sw(i)]))], 1u);
-  __syncthreads();
-  for (uint32_t b = tid; b < kHist; b += T)
-    if (shist[b]) atomicAdd(&gh[b], shist[b]);
-  cl.sync();
-  for (uint32_t b = tid; b < kHist; b += T) shist[b] = __ldcg(gh + b);
-  __syncthreads();
-  const float thr = threshold_from_hist(shist, n, a.factor, s_red);
-  // Bins above the threshold's bucket bound the beam's hot bins; the bound
-  // is the same in every CTA (same histogram), so the choice below is uniform.
-  const uint32_t tb = bucket_of(thr);
-  uint32_t hot_bound = 0;
-  for (uint32_t b = tid; b < kHist; b += T) hot_bound += b >= tb ? shist[b] : 0u;
-  uint32_t hot_total = 0;
-  (void)block_exclusive_scan(hot_bound, s_red, &hot_total);
-  const bool keep_records = hot_total <= list_cap;
-  // 2. classify own hot bins (|X| > thr) against both neighbours, read from
-  //    their CTAs; record (i, y_l, y_r) of the maxima for the output.
-  auto mag_at = [&](uint32_t k) -> float {
-    const uint32_t cc = k % C;
-    const float2* src = cc == c ? s : cl.map_shared_rank(s, cc);
-    return mag_rn(src[sw(k / C)]);
-  };
-  const uint32_t words = (M + 31) / 32;
-  uint32_t* mywords = shot;  // own maxima bits, bit l of word w <-> i = 32w + l
-  float* rec = reinterpret_cast<float*>(slist);  // [list_cap][3] = {i, y_l, y_r}
-  uint32_t* s_nrec = s_red + 100;
-  for (uint32_t w = tid; w < words; w += T) mywords[w] = 0;
-  if (tid == 0) *s_nrec = 0;
-  __syncthreads();
-  for (uint32_t i = i_start + tid; i < i_end; i += T) {
-    const float v = mag_rn(s[sw(i)]);
-    if (!(v > thr)) continue;
-    const uint32_t k = c + C * i;
-    const float yl = mag_at(k - 1), yr = mag_at(k + 1);
-    if (v > yl && v > yr) {
-      atomicOr(&mywords[i >> 5], 1u << (i & 31));
-      if (keep_records) {
-        const uint32_t r = atomicAdd(s_nrec, 1u);
-        rec[3 * r] = __uint_as_float(i);
-        rec[3 * r + 1] = yl;
-        rec[3 * r + 2] = yr;
+  *total = __shfl_sync(0xffffffffu, x, 31);
+  uint32_t found = 0xFFFFFFFFu, fbelow = 0;
+  uint32_t bl = below + x - sum;
+  if (bl <= r && r < below + x) {
+    for (uint32_t j = lo; j < hi; ++j) {
+      const uint32_t cnt = h[j];
+      if (bl <= r && r < bl + cnt) {
+        found = j;
+        fbelow = bl;
+        break;
       }
+      bl += cnt;
     }
   }
-  __syncthreads();
-  const size_t beam_words = (size_t)(g.nfft + 31) / 32 + C;
-  uint32_t* gm = a.gbits + (size_t)beam * beam_words;  // maxima bitmaps of the cluster
-  for (uint32_t w = tid; w < words; w += T) __stcg(gm + (size_t)c * words + w, mywords[w]);
-  cl.sync();
-  // 3. maxima of the whole beam in bin order, prefix popcount per 1024-bin block
-  const uint32_t kwords = (g.nfft + 31) / 32;
-  uint32_t* maxbits = shist;
-  for (uint32_t w = tid; w < kwords; w += T) maxbits[w] = 0;
-  __syncthreads();
-  for (uint32_t cw = tid; cw < C * words; cw += T) {
-    const uint32_t cc = cw / words, wi = cw % words;
-    for (uint32_t t = __ldcg(gm + cw); t; t &= t - 1) {
-      const uint32_t k = cc + C * (32 * wi + (__ffs(t) - 1));
-      atomicOr(&maxbits[k >> 5], 1u << (k & 31));
-    }
-  }
-  __syncthreads();
-  const uint32_t kblocks = (kwords + 31) / 32;  // <= 128
-  uint32_t* pref = s_red + 128;
-  for (uint32_t blk0 = 0; blk0 < kblocks; blk0 += T / 32) {
-    const uint32_t blk = blk0 + (tid >> 5);
-    const uint32_t w = blk * 32 + lane;
-    uint32_t v = (blk < kblocks && w < kwords) ? __popc(maxbits[w]) : 0u;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0 && blk < kblocks) pref[blk] = v;
-  }
-  __syncthreads();
-  if (tid < 32) {  // exclusive scan of <= 128 block sums, 4 per lane
-    uint32_t v[4], sum = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t blk = tid * 4 + j;
-      v[j] = blk < kblocks ? pref[blk] : 0u;
-      sum += v[j];
-    }
-    uint32_t x = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (tid >= (uint32_t)o) x += y;
-    }
-    uint32_t run = x - sum;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t blk = tid * 4 + j;
-      if (blk < kblocks) pref[blk] = run;
-      run += v[j];
-    }
-    if (tid == 31) s_red[64] = x;
-  }
-  __syncthreads();
-  if (c == 0 && tid == 0) a.counts[beam] = s_red[64];
-  // 4. own maxima -> MaxValue at their rank
-  const float bw = __fdiv_rn(a.fs, (float)g.nfft);
-  auto write_max = [&](uint32_t i, float yl, float yr) {
-    const uint32_t k = c + C * i;
-    uint32_t rank = pref[k >> 10];
-    for (uint32_t w2 = (k >> 10) << 5; w2 < (k >> 5); ++w2) rank += __popc(maxbits[w2]);
-    rank += __popc(maxbits[k >> 5] & ((1u << (k & 31)) - 1u));
-    if (rank < a.cap) {
-      const float2 z = s[sw(i)];
-      a.out[(size_t)beam * a.cap + rank] = fused_max(k, z, yl, mag_rn(z), yr, bw, a.refine);
-    }
-  };
-  if (keep_records) {
-    const uint32_t nrec = *s_nrec;
-    for (uint32_t r = tid; r < nrec; r += T)
-      write_max(__float_as_uint(rec[3 * r]), rec[3 * r + 1], rec[3 * r + 2]);
-    return;  // no DSMEM access after the last barrier
-  }
-  for (uint32_t w = tid; w < words; w += T)
-    for (uint32_t t = mywords[w]; t; t &= t - 1) {
-      const uint32_t i = 32 * w + (__ffs(t) - 1), k = c + C * i;
-      write_max(i, mag_at(k - 1), mag_at(k + 1));
-    }
-  cl.sync();  // (many maxima) other CTAs read this CTA's shared memory above
+  const uint32_t fl = __ballot_sync(0xffffffffu, found != 0xFFFFFFFFu);
+  if (!fl) return false;
+  const int src = __ffs(fl) - 1;
+  const uint32_t j = __shfl_sync(0xffffffffu, found, src);
+  const uint32_t bb = __shfl_sync(0xffffffffu, fbelow, src);
+  const uint32_t bk = b0 + j;
+  const float flo = __uint_as_float(bk << 19);
+  const float fhi = __uint_as_float((bk + 1) << 19);
+  const float frac = __fdiv_rn(__fadd_rn((float)(r - bb), 0.5f), (float)h[j]);
+  const float med = __fadd_rn(flo, __fmul_rn(__fsub_rn(fhi, flo), frac));
+  *thr = __fmul_rn(med, factor);
+  return true;
 }
 
 template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_peaks_kernel(FftGeom g, FusedArgs a) {
   extern __shared__ float2 s[];
-  // layout (u32 after the spectrum): histogram / maxima bitmap [4096 + 64] |
-  // reductions [256] | own maxima bits [ceil(M/32)] | maxima records [3 * kList]
+  // C == 1, after the spectrum: histogram / top-K lists [4096 + 64] | reductions [256]
   uint32_t* shist = reinterpret_cast<uint32_t*>(s + g.Mpad);
   uint32_t* s_red = shist + kHist + 64;
-  uint32_t* shot = s_red + 256;
-  uint32_t* slist = shot + (g.M + 31) / 32;
   const uint32_t tid = threadIdx.x, T = blockDim.x;
-  for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
   if (g.C == 1) {
+    for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
     const uint32_t beam = blockIdx.x;
     prefetch_future_beam(g, a.in, a.n_point, beam, 0, tid, T);
     local_fft<EPT>(s, g, SampleLoader{a.in + (size_t)beam * a.n_point, a.n_point, a.win}, a.tw_local, tid, T);
@@ -413,24 +291,316 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
     default: cross_stage_exchange<16>(slot, c, g.M, ld, a.tw_cross, tid, T); break;
   }
   cl.sync();
-  const float2* row = slot + (size_t)c * g.M;
+  float2* row = slot + (size_t)c * g.M;
   local_fft<EPT>(s, g, ExchangeLoader{row}, a.tw_local, tid, T);
-  discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
-  peaks_cluster(s, shist, s_red, shot, slist, kList, g, c, beam, a);
+  // Row c of the slot was read by this CTA alone and is dead: it now takes
+  // this CTA's bins k = c + C*i in [start - 1, end + 1) (the window and the
+  // neighbours of its end bins), row[i] = X[c + C*i].  The rest of the row is
+  // discarded from L2.
+  const uint32_t klo = a.start - 1, khi = min(a.end + 1, g.nfft);
+  const uint32_t ilo = klo <= c ? 0u : (klo - c + g.C - 1) / g.C;
+  const uint32_t ihi = khi <= c ? 0u : min(g.M, (khi - c + g.C - 1) / g.C);
+  for (uint32_t i = ilo + tid; i < ihi; i += T) __stcg(row + i, s[sw(i)]);
+  if (ihi > ilo) {
+    discard_row_l2(row, (size_t)ilo * sizeof(float2), tid, T);
+    discard_row_l2(row + ihi, (size_t)(g.M - ihi) * sizeof(float2), tid, T);
+  } else {
+    discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// maxima_cluster_kernel: every strict local maximum of |X| in [start, end)
+// above the per-beam threshold, compacted in bin order.  A cluster of C2
+// CTAs per beam; CTA c owns bins [start + c*chunk, start + (c+1)*chunk) and
+// keeps their |X| in shared memory:
+//  1. |X| of the CTA's bins and both neighbours of its range; with a
+//     threshold, a local histogram and its bucket range;
+//  2. (threshold) cluster barrier; the merged histogram over the union of the
+//     bucket ranges, read from every CTA through distributed shared memory;
+//     the threshold computed per warp;
+//  3. maxima flags (a bitmap in bin order) and their number, published in
+//     device memory; cluster barrier;
+//  4. rank of a maximum = maxima of the lower CTAs + maxima before it in
+//     this CTA; records written for ranks below the capacity.
+// The spectrum of beam b holds bin k at spec[b*nfft + (k mod C1)*M1 + k div C1]
+// (C1 = 1: natural order; C1 > 1: the cluster FFT's row layout).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMxThreads = 256;
+constexpr uint32_t kMxMinBlocks = 5;  // CTAs per SM the kernel is built for (<= 48 registers)
+constexpr uint32_t kMxMaxC2 = 8;
+constexpr uint32_t kMxMaxChunk = 32768;  // < 65536: 16-bit histogram counters cannot overflow
+constexpr uint32_t kMxBatch = 8;         // loads in flight per thread
+constexpr uint32_t kMxMerge = 512;       // buckets of the merged histogram per window
+
+struct MxArgs {
+  const float2* spec;
+  uint32_t* ccount;      // [beams][C2] maxima per CTA (scratch)
+  MaxValueDev* out;
+  uint32_t* counts;
+  uint32_t C1, M1;
+  uint32_t c1shift;      // log2(C1) when C1 is a power of two, else 32
+  uint32_t c1magic;      // ceil(2^32 / C1) (C1 not a power of two)
+  uint32_t nfft, start, end, cap, refine, chunk;
+  float fs, factor;      // factor <= 0: no threshold
+};
+
+// Bin k of a beam's spectrum (offsets < nfft <= 2^20 fit 32 bits).
+SPX_DEV float2 mx_load(const MxArgs& a, const float2* __restrict__ sb, uint32_t k) {
+  uint32_t q, r;
+  if (a.c1shift < 32) {
+    q = k >> a.c1shift;
+    r = k & (a.C1 - 1);
+  } else {
+    q = __umulhi(k, a.c1magic);  // k div C1 (exact: k * C1 < 2^32)
+    r = k - q * a.C1;
+  }
+  return __ldcs(sb + (r * a.M1 + q));
+}
+
+// Shared memory (32-bit words): |X| [chunk + 2] | maxima bits [chunk/32] |
+// reductions [64] | with a threshold: 16-bit histogram [kHist/2] | merged
+// window [kMxMerge].
+static size_t mx_smem_words(uint32_t chunk, bool thr) {
+  return (size_t)chunk + 2 + (chunk + 31) / 32 + 64 + (thr ? kHist / 2 + kMxMerge : 0);
+}
+
+__global__ void __launch_bounds__(kMxThreads, kMxMinBlocks)
+maxima_cluster_kernel(MxArgs a) {
+  extern __shared__ uint32_t smx[];
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t C2 = cl.num_blocks(), c = cl.block_rank(), beam = blockIdx.x / C2;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool thr_on = a.factor > 0.0f;
+  float* smag = reinterpret_cast<float*>(smx);         // [chunk + 2]: bins lo - 1 .. hi
+  uint32_t* bits = smx + a.chunk + 2;                   // [chunk / 32]
+  uint32_t* red = bits + (a.chunk + 31) / 32;           // [64]
+  uint32_t* hist = red + 64;                            // [kHist / 2]: bucket b in half b & 1 of word b / 2
+  uint32_t* merged = hist + kHist / 2;                  // [kMxMerge]
+  const uint32_t lo = min(a.start + c * a.chunk, a.end);
+  const uint32_t hi = min(lo + a.chunk, a.end);
+  const uint32_t nb = hi - lo;
+  const float2* sb = a.spec + (size_t)beam * a.nfft;
+  if (thr_on) {
+    for (uint32_t b = tid; b < kHist / 2; b += kMxThreads) hist[b] = 0;
+    if (tid == 0) {
+      red[0] = kHist;
+      red[1] = 0;
+    }
+    __syncthreads();
+  }
+  // 1. (loads issued kMxBatch at a time per thread, so that enough bytes
+  //    are in flight to cover the device-memory latency)
+  uint32_t bmin = kHist, bmax = 0;
+  const uint32_t nload = nb ? nb + 2 : 0;
+  for (uint32_t i0 = 0; i0 < nload; i0 += kMxBatch * kMxThreads) {
+    float2 z[kMxBatch];
+#pragma unroll
+    for (uint32_t j = 0; j < kMxBatch; ++j) {
+      const uint32_t i = i0 + j * kMxThreads + tid;
+      if (i < nload) z[j] = mx_load(a, sb, lo - 1 + i);
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kMxBatch; ++j) {
+      const uint32_t i = i0 + j * kMxThreads + tid;
+      if (i < nload) {
+        const float m = mag_rn(z[j]);
+        smag[i] = m;
+        if (thr_on && i >= 1 && i <= nb) {
+          const uint32_t b = bucket_of(m);
+          atomicAdd(&hist[b >> 1], 1u << ((b & 1u) * 16));
+          bmin = min(bmin, b);
+          bmax = max(bmax, b);
+        }
+      }
+    }
+  }
+  float thr = -INFINITY;
+  if (thr_on) {
+    bmin = __reduce_min_sync(0xffffffffu, bmin);
+    bmax = __reduce_max_sync(0xffffffffu, bmax);
+    if (lane == 0 && bmin <= bmax) {
+      atomicMin(&red[0], bmin);
+      atomicMax(&red[1], bmax);
+    }
+    __syncthreads();
+    cl.sync();  // every histogram complete; read remotely until the next cluster barrier
+    // 2.
+    if (warp == 0) {
+      uint32_t l = kHist, h = 0;
+      if (lane < C2) {
+        const uint32_t* r = cl.map_shared_rank(red, lane);
+        l = r[0];
+        h = r[1];
+      }
+      l = __reduce_min_sync(0xffffffffu, l);
+      h = __reduce_max_sync(0xffffffffu, h);
+      if (lane == 0) {
+        red[2] = l;
+        red[3] = h;
+      }
+    }
+    __syncthreads();
+    const uint32_t b0 = red[2];
+    const uint32_t R = b0 <= red[3] ? red[3] - b0 + 1 : 0u;
+    const uint32_t n = a.end > a.start ? a.end - a.start : 0u;
+    thr = INFINITY;
+    // the merged histogram in windows of kMxMerge buckets (one window unless
+    // |X| spans more than 2^(kMxMerge/16) in ratio); same steps in every CTA
+    uint32_t below = 0;
+    for (uint32_t w0 = 0; n > 0 && w0 < R; w0 += kMxMerge) {
+      const uint32_t W = min(kMxMerge, R - w0);
+      for (uint32_t t = tid; t < W; t += kMxThreads) {
+        const uint32_t b = b0 + w0 + t;
+        uint32_t sum = 0;
+#pragma unroll
+        for (uint32_t cc = 0; cc < kMxMaxC2; ++cc)
+          if (cc < C2) sum += (cl.map_shared_rank(hist, cc)[b >> 1] >> ((b & 1u) * 16)) & 0xFFFFu;
+        merged[t] = sum;
+      }
+      __syncthreads();
+      uint32_t wtot = 0;
+      const bool done = warp_median_window(merged, W, b0 + w0, below, (n - 1) / 2, a.factor, &thr, &wtot);
+      __syncthreads();  // merged rewritten by the next window
+      if (done) break;
+      below += wtot;
+    }
+  } else {
+    __syncthreads();
+  }
+  // 3. bins lo + u*256 + warp*32 + lane -> bit lane of word u*8 + warp
+  const uint32_t words = (nb + 31) / 32;
+  for (uint32_t u = 0; u * kMxThreads < nb; ++u) {
+    const uint32_t i = u * kMxThreads + tid;
+    bool f = false;
+    if (i < nb) {
+      const float v = smag[i + 1];
+      f = (v > smag[i]) && (v > smag[i + 2]) && (v > thr);
+    }
+    const uint32_t b = __ballot_sync(0xffffffffu, f);
+    const uint32_t w = u * (kMxThreads / 32) + warp;
+    if (lane == 0 && w < words) bits[w] = b;
+  }
+  __syncthreads();
+  // contiguous words per thread, block-wide exclusive scan of their maxima
+  const uint32_t per = (words + kMxThreads - 1) / kMxThreads;
+  const uint32_t w0 = min(tid * per, words), w1 = min(w0 + per, words);
+  uint32_t mine = 0;
+  for (uint32_t w = w0; w < w1; ++w) mine += __popc(bits[w]);
+  uint32_t x = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) red[8 + warp] = x;
+  __syncthreads();
+  uint32_t before = 0, own = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < kMxThreads / 32; ++w) {
+    const uint32_t v = red[8 + w];
+    before += w < warp ? v : 0u;
+    own += v;
+  }
+  uint32_t rank = before + x - mine;
+  uint32_t* cc_counts = a.ccount + (size_t)beam * C2;
+  if (C2 > 1) {
+    if (tid == 0) __stcg(cc_counts + c, own);
+    cl.sync();  // counts visible; no distributed shared memory access after this barrier
+  }
+  uint32_t base = 0, total = own;
+  if (C2 > 1) {
+    total = 0;
+    for (uint32_t cc = 0; cc < C2; ++cc) {
+      const uint32_t v = __ldcg(cc_counts + cc);
+      base += cc < c ? v : 0u;
+      total += v;
+    }
+  }
+  if (c == 0 && tid == 0) a.counts[beam] = total;
+  // 4.
+  rank += base;
+  if (rank >= a.cap) return;
+  const float bw = __fdiv_rn(a.fs, (float)a.nfft);
+  MaxValueDev* o = a.out + (size_t)beam * a.cap;
+  for (uint32_t w = w0; w < w1 && rank < a.cap; ++w) {
+    for (uint32_t t = bits[w]; t && rank < a.cap; t &= t - 1) {
+      const uint32_t i = 32 * w + (__ffs(t) - 1), k = lo + i;
+      o[rank++] = fused_max(k, mx_load(a, sb, k), smag[i], smag[i + 1], smag[i + 2], bw, a.refine);
+    }
+  }
 }
 
 // Shared memory of the fused kernel for geometry g.
 static size_t fused_smem(const FftGeom& g) {
-  const size_t hot = g.C > 1 ? (size_t)(g.M + 31) / 32 + 3 * kList : 0;
-  return (size_t)g.Mpad * sizeof(float2) + (kHist + 64 + 256 + hot) * sizeof(uint32_t);
+  return (size_t)g.Mpad * sizeof(float2) + (g.C == 1 ? (kHist + 64 + 256) * sizeof(uint32_t) : 0);
+}
+
+// Cluster size and bins per CTA of maxima_cluster_kernel for a window of `span` bins.
+static bool mx_geometry(uint32_t span, uint32_t* C2, uint32_t* chunk) {
+  uint32_t c2 = (span + 8191) / 8192;
+  if (c2 < 1) c2 = 1;
+  if (c2 > kMxMaxC2) c2 = kMxMaxC2;
+  uint32_t ch = (span + c2 - 1) / c2;
+  ch = (ch + 31) & ~31u;
+  if (ch == 0) ch = 32;
+  if (ch > kMxMaxChunk) return false;
+  *C2 = c2;
+  *chunk = ch;
+  return true;
 }
 
 bool fused_supported(const FftGeom& g, uint32_t mode) {
-  if (mode == SPX_PEAK_TOPK) return g.C == 1;
-  if (mode != SPX_PEAK_ALL) return false;
-  if ((g.nfft + 31) / 32 > kHist) return false;  // maxima bitmap lives in the histogram area
-  if ((g.nfft + 31) / 32 > 128 * 32) return false;  // block prefix table holds 128 entries
-  return (kHist % g.T) == 0 && g.T <= kList && fused_smem(g) <= 227 * 1024;
+  if (mode != SPX_PEAK_ALL && mode != SPX_PEAK_TOPK) return false;
+  if (g.C == 1) return (kHist % g.T) == 0 && fused_smem(g) <= 227 * 1024;
+  if (mode == SPX_PEAK_TOPK) return false;
+  uint32_t c2, ch;
+  return mx_geometry(g.nfft, &c2, &ch) && g.C <= 16;
+}
+
+spx_status launch_maxima_cluster(spx_ctx* ctx, const float2* d_spec, uint32_t C1, uint32_t M1,
+                                 uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                                 uint32_t cap, float fs, uint32_t refine, float factor,
+                                 uint32_t* d_ccount, spx_max_value* d_out, uint32_t* d_counts) {
+  if (beams == 0) return SPX_OK;
+  uint32_t C2 = 1, chunk = 32;
+  if (!mx_geometry(end > start ? end - start : 0u, &C2, &chunk))
+    return fail(ctx, SPX_ERR_INVALID_ARG, "maxima: search window too long");
+  MxArgs a{};
+  a.spec = d_spec;
+  a.ccount = d_ccount;
+  a.out = reinterpret_cast<MaxValueDev*>(d_out);
+  a.counts = d_counts;
+  a.C1 = C1;
+  a.M1 = M1;
+  a.c1shift = (C1 & (C1 - 1)) == 0 ? (uint32_t)__builtin_ctz(C1) : 32u;
+  a.c1magic = a.c1shift == 32 ? (uint32_t)(((1ull << 32) + C1 - 1) / C1) : 0u;
+  a.nfft = nfft;
+  a.start = start;
+  a.end = end;
+  a.cap = cap;
+  a.refine = refine;
+  a.chunk = chunk;
+  a.fs = fs;
+  a.factor = factor;
+  const size_t smem = mx_smem_words(chunk, factor > 0.0f) * sizeof(uint32_t);
+  cudaError_t e = configure_kernel((const void*)maxima_cluster_kernel, 227 * 1024);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "configure maxima_cluster_kernel");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(beams * C2, 1, 1);
+  cfg.blockDim = dim3(kMxThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, maxima_cluster_kernel, a);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch maxima_cluster_kernel");
+  return SPX_OK;
 }
 
 spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
@@ -456,26 +626,19 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   a.refine = refine;
   a.fs = fs;
   a.factor = factor;
-  cudaError_t e;
+  uint32_t* ccount = nullptr;
   if (g.C > 1) {
-    const size_t xch_bytes = (size_t)beams * g.nfft * sizeof(float2);
-    const size_t hist_bytes = (size_t)beams * kHist * sizeof(uint32_t);
-    const size_t bits_bytes = (size_t)beams * ((g.nfft + 31) / 32 + g.C) * sizeof(uint32_t);
+    const size_t xch_bytes = ((size_t)beams * g.nfft * sizeof(float2) + 255) & ~(size_t)255;
     void* p = nullptr;
-    spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + hist_bytes + bits_bytes + 512, &p);
+    spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + (size_t)beams * kMxMaxC2 * sizeof(uint32_t), &p);
     if (st != SPX_OK) return st;
-    char* base = static_cast<char*>(p);
-    a.xch = reinterpret_cast<float2*>(base);
-    a.ghist = reinterpret_cast<uint32_t*>(base + ((xch_bytes + 255) & ~(size_t)255));
-    a.gbits = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.ghist) +
-                                          ((hist_bytes + 255) & ~(size_t)255));
-    e = cudaMemsetAsync(a.ghist, 0, hist_bytes, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(histograms)");
+    a.xch = static_cast<float2*>(p);
+    ccount = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes);
   }
   void* args[] = {(void*)&g, (void*)&a};
   const size_t smem = fused_smem(g);
   const void* kfn = g.ept == 32 ? (const void*)fft_peaks_kernel<32> : (const void*)fft_peaks_kernel<16>;
-  e = configure_kernel(kfn, 227 * 1024);
+  cudaError_t e = configure_kernel(kfn, 227 * 1024);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
   g.beams = beams;
   g.ahead = ctx->input_on_host ? 0u : resident_beams(kfn, g, smem);
@@ -495,7 +658,9 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   }
   e = cudaLaunchKernelExC(&cfg, kfn, args);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_peaks_kernel");
-  return SPX_OK;
+  if (g.C == 1) return SPX_OK;
+  return launch_maxima_cluster(ctx, a.xch, g.C, g.M, beams, g.nfft, start, end, cap_or_k, fs, refine,
+                               factor, ccount, d_out, d_counts);
 }
 
 }  // namespace spx

@@ -405,8 +405,9 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
   const FftPlan* plan = nullptr;
   spx_status st = get_plan(ctx, nfft, &plan);
   if (st != SPX_OK) return st;
-  // Fused single launch (the spectrum stays on chip) for ALL maxima (C == 1,
-  // or C > 1 with a noise threshold) and TOP-K (C == 1).
+  // Fused path: ALL maxima and TOP-K in one launch for C == 1 (the spectrum
+  // stays on chip); ALL maxima for C > 1 as the cluster FFT, which writes the
+  // window's bins, and the maxima cluster kernel.
   if (params->mode == SPX_PEAK_ALL || params->mode == SPX_PEAK_TOPK) {
     st = peak_common_checks(ctx, params, nfft);
     if (st != SPX_OK) return st;
@@ -422,7 +423,7 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
       cap = params->max_per_beam;
     }
     const bool thr = params->thresh_sigma > 0.0f;
-    if (!plan->big && fused_supported(plan->g, params->mode) && (!all || plan->g.C == 1 || thr)) {
+    if (!plan->big && fused_supported(plan->g, params->mode)) {
       const float* win = nullptr;
       st = get_window(ctx, window, n_point, &win);
       if (st != SPX_OK) return st;

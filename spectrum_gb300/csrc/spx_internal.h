@@ -96,6 +96,13 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
                             uint32_t* d_counts);
+// All maxima of spectra whose bin k of beam b sits at
+// d_spec[b*nfft + (k mod C1)*M1 + k div C1] (C1 = 1: natural order), with the
+// noise threshold when factor > 0; d_ccount holds beams * 8 words of scratch.
+spx_status launch_maxima_cluster(spx_ctx* ctx, const float2* d_spec, uint32_t C1, uint32_t M1,
+                                 uint32_t beams, uint32_t nfft, uint32_t start, uint32_t end,
+                                 uint32_t cap, float fs, uint32_t refine, float factor,
+                                 uint32_t* d_ccount, spx_max_value* d_out, uint32_t* d_counts);
 
 // Kernel launchers (fft_kernels.cu, peak_kernels.cu).
 spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,

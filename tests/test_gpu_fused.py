@@ -51,6 +51,24 @@ def test_fused_all_maxima_thresholded(spx, cuda, nfft, n_point, beams, refine):
     assert rc.min() >= 1
 
 
+@pytest.mark.parametrize("nfft,n_point,sigma,start,end", [(131072, 65536, 0.5, 0, 0), (65536, 65536, 1.0, 0, 0),
+                                                         (131072, 100000, 2.0, 5000, 120000),
+                                                         (39366, 39366, 0.25, 3, 39000)])
+def test_fused_cluster_many_hot_bins(spx, cuda, nfft, n_point, sigma, start, end):
+    """Low thresholds: thousands of bins above the threshold's bucket, so the
+    cluster epilogue takes its bitmap path; lists equal to the oracle's."""
+    import torch
+    x = _beams(3, n_point, nfft + int(sigma * 8))
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_ALL, sample_rate=48000.0, refine=1,
+                                thresh_sigma=sigma, search_start=start, search_end=end)
+    ref, rc = orc.all_maxima(None, spec, nfft, 48000.0, start, end, refine=1, thresh_sigma=sigma)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+    assert rc.min() > 1024 // 8
+
+
 @pytest.mark.parametrize("nfft,start,end,cap", [(4096, 0, 0, 1000), (8192, 100, 3000, 64), (2048, 1, 2047, 10)])
 def test_fused_all_maxima_reference_semantics_single_cta(spx, cuda, nfft, start, end, cap):
     """No threshold (every strict local maximum), C = 1: still one fused launch."""
