@@ -392,21 +392,21 @@ maxima_cluster_kernel(MxArgs a) {
   // 1. (loads issued kMxBatch at a time per thread, so that enough bytes
   //    are in flight to cover the device-memory latency)
   uint32_t bmin = kHist, bmax = 0;
-  const uint32_t nload = nb ? nb + 2 : 0;
-  for (uint32_t i0 = 0; i0 < nload; i0 += kMxBatch * kMxThreads) {
+  if (nb && tid < 2) smag[tid ? nb + 1 : 0] = mag_rn(mx_load(a, sb, tid ? hi : lo - 1));  // neighbours
+  for (uint32_t i0 = 0; i0 < nb; i0 += kMxBatch * kMxThreads) {
     float2 z[kMxBatch];
 #pragma unroll
     for (uint32_t j = 0; j < kMxBatch; ++j) {
       const uint32_t i = i0 + j * kMxThreads + tid;
-      if (i < nload) z[j] = mx_load(a, sb, lo - 1 + i);
+      if (i < nb) z[j] = mx_load(a, sb, lo + i);
     }
 #pragma unroll
     for (uint32_t j = 0; j < kMxBatch; ++j) {
       const uint32_t i = i0 + j * kMxThreads + tid;
-      if (i < nload) {
+      if (i < nb) {
         const float m = mag_rn(z[j]);
-        smag[i] = m;
-        if (thr_on && i >= 1 && i <= nb) {
+        smag[i + 1] = m;
+        if (thr_on) {
           const uint32_t b = bucket_of(m);
           atomicAdd(&hist[b >> 1], 1u << ((b & 1u) * 16));
           bmin = min(bmin, b);
