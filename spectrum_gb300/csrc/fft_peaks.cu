@@ -331,6 +331,7 @@ constexpr uint32_t kMxMinBlocks = 5;  // CTAs per SM the kernel is built for (<=
 constexpr uint32_t kMxMaxC2 = 8;
 constexpr uint32_t kMxMaxChunk = 32768;  // < 65536: 16-bit histogram counters cannot overflow
 constexpr uint32_t kMxBatch = 8;         // loads in flight per thread
+static_assert(kMxMaxC2 * kMxMaxChunk == kMaxClusterSpan, "window limit of spx_all_maxima");
 constexpr uint32_t kMxMerge = 512;       // buckets of the merged histogram per window
 
 struct MxArgs {

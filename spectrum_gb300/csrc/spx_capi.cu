@@ -360,6 +360,16 @@ spx_status spx_all_maxima(spx_ctx* ctx, const float* d_mag, const void* d_fft, u
                           &start, &end, &cap);
   if (cap > 0 && !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_all_maxima: out is null");
   DeviceGuard g(ctx->device);
+  if (!d_mag && (end > start ? end - start : 0u) <= kMaxClusterSpan) {
+    // one launch: |X|, noise threshold, maxima and ranks (maxima_cluster_kernel)
+    void* scratch = nullptr;
+    st = get_scratch(ctx, kSlotWork, (size_t)beams * 8 * sizeof(uint32_t), &scratch);
+    if (st != SPX_OK) return st;
+    const float factor = params->thresh_sigma > 0.0f ? spx_noise_threshold_factor(params->thresh_sigma) : 0.0f;
+    return launch_maxima_cluster(ctx, static_cast<const float2*>(d_fft), 1, nfft, beams, nfft, start, end, cap,
+                                 params->sample_rate, params->refine, factor,
+                                 static_cast<uint32_t*>(scratch), d_out, d_counts);
+  }
   const float* thr = nullptr;
   st = thresholds(ctx, d_mag, static_cast<const float2*>(d_fft), beams, nfft, start, end,
                   params->thresh_sigma, &thr);

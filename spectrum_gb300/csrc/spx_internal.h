@@ -96,6 +96,8 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
                             uint32_t* d_counts);
+// Longest search window maxima_cluster_kernel takes (8 CTAs x 32768 bins).
+constexpr uint32_t kMaxClusterSpan = 8u * 32768u;
 // All maxima of spectra whose bin k of beam b sits at
 // d_spec[b*nfft + (k mod C1)*M1 + k div C1] (C1 = 1: natural order), with the
 // noise threshold when factor > 0; d_ccount holds beams * 8 words of scratch.
