@@ -36,9 +36,9 @@ BEAMS, N_POINT, NFFT = 256, 65536, 131072
 FS = 1.0
 SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
-# DRAM bytes (read + write) of one fft_peaks_kernel launch on this workload,
-# from an ncu capture (profiles/fft_peaks_kernel_plain_large.md).
-NCU_TRAFFIC_BYTES = 143_483_392
+# DRAM bytes (read + write) of one step on this workload (fft_peaks_kernel +
+# maxima_cluster_kernel), from an ncu capture (profiles/fft_peaks_kernel_plain_large.md).
+NCU_TRAFFIC_BYTES = 359_455_744
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
@@ -345,8 +345,9 @@ def run_gpu(args):
 
 
 def time_components(spx, ctx, xs, out, counts, p, stream, steps):
-    """Times the dominant kernel of a step (the fused FFT + peak kernel) with
-    CUDA events on the launching stream, plus the composed path's kernels."""
+    """Times a step (the FFT kernel and the maxima kernel, back to back on one
+    stream) with CUDA events on the launching stream, plus the composed path
+    (spx_fft to a spectrum in device memory, then spx_all_maxima)."""
     import ctypes as C
 
     import torch
@@ -382,17 +383,20 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
     # algorithmic bytes: samples read once + maxima and counts written
     algo = BEAMS * N_POINT * 8 + n_max * 32 + BEAMS * 4
     return {
-        "path": "fused: fft_peaks_kernel (one cluster of 8 CTAs x 1024 threads per beam; FFT, |X|, "
-                "threshold, maxima and compaction on chip) after a 4 MiB histogram memset",
+        "path": "spx_fft_peaks: fft_peaks_kernel (one cluster of 8 CTAs x 1024 threads per beam: window, "
+                "zero pad, 131072-point FFT; the search window's bins in row layout into the beam's L2 "
+                "exchange slot) then maxima_cluster_kernel (one cluster of 8 CTAs x 256 threads per beam, "
+                "5 CTAs per SM: |X|, noise histogram merged through DSMEM, 6-sigma threshold, maxima, ranks)",
         "components_ms": {"fused_step": round(f, 4), "composed_fft_complex": round(statistics.median(fft_ms), 4),
                           "composed_peaks": round(statistics.median(peak_ms), 4)},
-        "roofline": {"bound": "hbm", "kernel": "fft_peaks_kernel", "achieved": round(algo / (f * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "kernel": "fft_peaks_kernel + maxima_cluster_kernel (one step)",
+                     "achieved": round(algo / (f * 1e-3) / 1e9, 1),
                      "unit": "GB/s", "traffic": NCU_TRAFFIC_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
-                                       "(profiles/fft_peaks_kernel_plain_large.md)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of each "
+                                       "kernel (profiles/fft_peaks_kernel_plain_large.md)",
                      "algorithmic_bytes_per_launch": algo,
                      "maxima_per_launch": n_max},
-        "launches_per_step": 1,
+        "launches_per_step": 2,
     }
 
 
