@@ -42,6 +42,8 @@ struct FusedArgs {
   const float2* tw_local;
   const float2* tw_cross;
   float2* xch;              // exchange slots (C > 1), one per beam; then the window's bins
+  uint32_t* arrive;         // [beams] group-barrier arrivals (C > 1), zeroed by the host
+  uint32_t* err;            // device error word
   MaxValueDev* out;
   uint32_t* counts;
   uint32_t n_point, start, end, cap, mode, K, refine;
@@ -258,6 +260,24 @@ SPX_DEV bool warp_median_window(const uint32_t* h, uint32_t W, uint32_t b0, uint
   return true;
 }
 
+// Row c of a beam's exchange slot (read by this CTA alone, dead after its
+// local FFT) takes this CTA's bins k = c + C*i in [start - 1, end + 1) (the
+// search window and the neighbours of its end bins): row[i] = X[c + C*i].
+// The rest of the row is discarded from L2.
+SPX_DEV void write_window_row(float2* row, const float2* s, const FftGeom& g, uint32_t c, uint32_t start,
+                              uint32_t end, uint32_t tid, uint32_t T) {
+  const uint32_t klo = start - 1, khi = min(end + 1, g.nfft);
+  const uint32_t ilo = klo <= c ? 0u : (klo - c + g.C - 1) / g.C;
+  const uint32_t ihi = khi <= c ? 0u : min(g.M, (khi - c + g.C - 1) / g.C);
+  for (uint32_t i = ilo + tid; i < ihi; i += T) __stcg(row + i, s[sw(i)]);
+  if (ihi > ilo) {
+    discard_row_l2(row, (size_t)ilo * sizeof(float2), tid, T);
+    discard_row_l2(row + ihi, (size_t)(g.M - ihi) * sizeof(float2), tid, T);
+  } else {
+    discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
+  }
+}
+
 template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_peaks_kernel(FftGeom g, FusedArgs a) {
@@ -274,6 +294,7 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
     peaks_single_cta(s, shist, s_red, g, beam, a);
     return;
   }
+  // C > 1 (sizes fft_group_kernel does not take): one cluster per beam
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t c = cl.block_rank();
   const uint32_t beam = blockIdx.x / g.C;
@@ -293,20 +314,66 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   cl.sync();
   float2* row = slot + (size_t)c * g.M;
   local_fft<EPT>(s, g, ExchangeLoader{row}, a.tw_local, tid, T);
-  // Row c of the slot was read by this CTA alone and is dead: it now takes
-  // this CTA's bins k = c + C*i in [start - 1, end + 1) (the window and the
-  // neighbours of its end bins), row[i] = X[c + C*i].  The rest of the row is
-  // discarded from L2.
-  const uint32_t klo = a.start - 1, khi = min(a.end + 1, g.nfft);
-  const uint32_t ilo = klo <= c ? 0u : (klo - c + g.C - 1) / g.C;
-  const uint32_t ihi = khi <= c ? 0u : min(g.M, (khi - c + g.C - 1) / g.C);
-  for (uint32_t i = ilo + tid; i < ihi; i += T) __stcg(row + i, s[sw(i)]);
-  if (ihi > ilo) {
-    discard_row_l2(row, (size_t)ilo * sizeof(float2), tid, T);
-    discard_row_l2(row + ihi, (size_t)(g.M - ihi) * sizeof(float2), tid, T);
-  } else {
-    discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
+  write_window_row(row, s, g, c, a.start, a.end, tid, T);
+}
+
+// Barrier of the C CTAs working on one beam (one cooperative launch, so all
+// CTAs are resident): every CTA adds one arrival to the beam's counter
+// (release) and waits until C have arrived (acquire), at most kSpinLimitNs,
+// then sets kErrLookbackTimeout and goes on.
+SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
+    r.fetch_add(1u, cuda::memory_order_release);
+    if (r.load(cuda::memory_order_acquire) < C) {
+      const uint64_t t0 = globaltimer_ns();
+      while (r.load(cuda::memory_order_acquire) < C) {
+        if (globaltimer_ns() - t0 > kSpinLimitNs) {
+          atomicOr(err, kErrLookbackTimeout);
+          break;
+        }
+      }
+    }
   }
+  __syncthreads();
+}
+
+// C > 1 with a power-of-two local size M (4096, 8192, 16384; M / 16 threads)
+// and C in {2, 4, 8, 16}: a persistent cooperative launch of G groups of C
+// CTAs (one CTA per SM); group q transforms beams q, q + G, ...  Per beam:
+// the cross stage into the beam's exchange slot, a group barrier, the local
+// FFT of row c, the window's bins into row c.  Clusters of 8 one-SM CTAs
+// fit on 120 of the 152 SMs; groups use all of them.
+template <int M>
+__global__ void __launch_bounds__(M / 16, 16384 / M)
+fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
+  extern __shared__ float2 s[];
+  constexpr uint32_t T = M / 16;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t grp = blockIdx.x / g.C, c = blockIdx.x - grp * g.C;
+#pragma unroll 1
+  for (uint32_t beam = grp; beam < g.beams; beam += groups) {
+    float2* slot = a.xch + (size_t)beam * g.nfft;
+    const SampleLoader ld{a.in + (size_t)beam * a.n_point, a.n_point, a.win};
+    prefetch_future_beam(g, a.in, a.n_point, beam, c, tid, T);
+    switch (g.C) {
+      case 2: cross_stage_exchange<2>(slot, c, M, ld, a.tw_cross, tid, T); break;
+      case 4: cross_stage_exchange<4>(slot, c, M, ld, a.tw_cross, tid, T); break;
+      case 8: cross_stage_exchange<8>(slot, c, M, ld, a.tw_cross, tid, T); break;
+      default: cross_stage_exchange<16>(slot, c, M, ld, a.tw_cross, tid, T); break;
+    }
+    group_barrier(a.arrive + beam, g.C, a.err);
+    float2* row = slot + (size_t)c * M;
+    p2_local_fft<M>(s, ExchangeLoader{row}, a.tw_local, tid);
+    write_window_row(row, s, g, c, a.start, a.end, tid, T);
+  }
+}
+
+static bool group_supported(const FftGeom& g) {
+  return g.C > 1 && (g.C & (g.C - 1)) == 0 && g.ept == 16 && (g.M == 4096 || g.M == 8192 || g.M == 16384) &&
+         g.T == g.M / 16;
 }
 
 // ---------------------------------------------------------------------------
@@ -618,6 +685,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   a.tw_cross = plan.d_tw_cross;
   a.out = reinterpret_cast<MaxValueDev*>(d_out);
   a.counts = d_counts;
+  a.err = ctx->d_error;
   a.n_point = n_point;
   a.start = start;
   a.end = end;
@@ -627,39 +695,74 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   a.refine = refine;
   a.fs = fs;
   a.factor = factor;
-  uint32_t* ccount = nullptr;
-  if (g.C > 1) {
-    const size_t xch_bytes = ((size_t)beams * g.nfft * sizeof(float2) + 255) & ~(size_t)255;
-    void* p = nullptr;
-    spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + (size_t)beams * kMxMaxC2 * sizeof(uint32_t), &p);
-    if (st != SPX_OK) return st;
-    a.xch = static_cast<float2*>(p);
-    ccount = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes);
-  }
-  void* args[] = {(void*)&g, (void*)&a};
   const size_t smem = fused_smem(g);
-  const void* kfn = g.ept == 32 ? (const void*)fft_peaks_kernel<32> : (const void*)fft_peaks_kernel<16>;
-  cudaError_t e = configure_kernel(kfn, 227 * 1024);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
   g.beams = beams;
-  g.ahead = ctx->input_on_host ? 0u : resident_beams(kfn, g, smem);
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(beams * g.C, 1, 1);
-  cfg.blockDim = dim3(g.T, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = ctx->stream;
-  cudaLaunchAttribute attr[1];
-  if (g.C > 1) {
+  cudaError_t e;
+  if (g.C == 1) {
+    const void* kfn = g.ept == 32 ? (const void*)fft_peaks_kernel<32> : (const void*)fft_peaks_kernel<16>;
+    e = configure_kernel(kfn, 227 * 1024);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
+    g.ahead = ctx->input_on_host ? 0u : resident_beams(kfn, g, smem);
+    void* args[] = {(void*)&g, (void*)&a};
+    e = cudaLaunchKernel(kfn, dim3(beams), dim3(g.T), args, smem, ctx->stream);
+    return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch fft_peaks_kernel");
+  }
+  // C > 1: scratch = exchange slots | per-CTA maxima counts | group-barrier arrivals
+  const size_t xch_bytes = ((size_t)beams * g.nfft * sizeof(float2) + 255) & ~(size_t)255;
+  const size_t cnt_bytes = ((size_t)beams * kMxMaxC2 * sizeof(uint32_t) + 255) & ~(size_t)255;
+  void* p = nullptr;
+  spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + cnt_bytes + (size_t)beams * sizeof(uint32_t), &p);
+  if (st != SPX_OK) return st;
+  a.xch = static_cast<float2*>(p);
+  uint32_t* ccount = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes);
+  a.arrive = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes + cnt_bytes);
+  if (group_supported(g)) {
+    e = cudaMemsetAsync(a.arrive, 0, (size_t)beams * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(group barriers)");
+    const void* kfn = g.M == 16384 ? (const void*)fft_group_kernel<16384>
+                      : g.M == 8192 ? (const void*)fft_group_kernel<8192>
+                                    : (const void*)fft_group_kernel<4096>;
+    e = configure_kernel(kfn, 227 * 1024);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_group_kernel");
+    // as many groups as can be resident at once (cooperative launch), at most one per beam
+    uint32_t groups = resident_ctas(kfn, g.T, smem, 1) / g.C;
+    if (groups > beams) groups = beams;
+    if (groups == 0) return fail(ctx, SPX_ERR_CUDA, "fft_group_kernel: a group of CTAs does not fit the device");
+    g.ahead = ctx->input_on_host ? 0u : groups;
+    void* args[] = {(void*)&g, (void*)&a, (void*)&groups};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(groups * g.C, 1, 1);
+    cfg.blockDim = dim3(g.T, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, kfn, args);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_group_kernel");
+  } else {
+    const void* kfn = g.ept == 32 ? (const void*)fft_peaks_kernel<32> : (const void*)fft_peaks_kernel<16>;
+    e = configure_kernel(kfn, 227 * 1024);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_peaks_kernel");
+    g.ahead = ctx->input_on_host ? 0u : resident_beams(kfn, g, smem);
+    void* args[] = {(void*)&g, (void*)&a};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(beams * g.C, 1, 1);
+    cfg.blockDim = dim3(g.T, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = g.C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, kfn, args);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_peaks_kernel");
   }
-  e = cudaLaunchKernelExC(&cfg, kfn, args);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_peaks_kernel");
-  if (g.C == 1) return SPX_OK;
   return launch_maxima_cluster(ctx, a.xch, g.C, g.M, beams, g.nfft, start, end, cap_or_k, fs, refine,
                                factor, ccount, d_out, d_counts);
 }

@@ -231,13 +231,6 @@ spx_status launch_one_two(spx_ctx* ctx, const float2* d_fft, uint32_t beams, uin
 constexpr uint32_t kAmThreads = 256;
 constexpr uint32_t kAmRounds = 8;
 constexpr uint32_t kAmTile = kAmThreads * kAmRounds;  // bins per tile
-constexpr uint64_t kSpinLimitNs = 1000000000ull;      // 1 s bound on any look-back wait
-
-SPX_DEV uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // Tile status word: epoch (32) | flag (2) | count (30).  flag 1 = tile
 // aggregate published, 2 = inclusive prefix published.  Words from another

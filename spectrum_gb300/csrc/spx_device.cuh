@@ -12,6 +12,15 @@
 
 namespace spx {
 
+// ---- bounded waits ------------------------------------------------------------
+constexpr uint64_t kSpinLimitNs = 1000000000ull;  // 1 s bound on any device-side wait
+
+SPX_DEV uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // ---- complex helpers -------------------------------------------------------
 SPX_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 SPX_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }

@@ -31,7 +31,7 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept = kEPTDefault,
 bool is_smooth23(uint32_t n);
 
 // Error word bits written by kernels into spx_ctx::d_error.
-constexpr uint32_t kErrLookbackTimeout = 1u;
+constexpr uint32_t kErrLookbackTimeout = 1u;  // a bounded device-side wait gave up (look-back, beam group barrier)
 
 }  // namespace spx
 
