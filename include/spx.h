@@ -151,6 +151,10 @@ int spx_abi_version(void);
  * This call runs one such wait on a predecessor that never publishes, so it
  * takes about 1 s and returns SPX_ERR_TIMEOUT; the context stays usable. */
 spx_status spx_selftest_wait_timeout(spx_ctx* ctx);
+/* The same for the per-beam group barrier of the large fused transform
+ * (nfft > 16384): one CTA waits for a second arrival that never comes;
+ * about 1 s, SPX_ERR_TIMEOUT, the context stays usable. */
+spx_status spx_selftest_group_wait_timeout(spx_ctx* ctx);
 
 /* ---- sizes -------------------------------------------------------------- */
 /* nextPow2(n) as the reference computes it (fft_processor_rocm.cpp:665-671); 0 -> 1. */

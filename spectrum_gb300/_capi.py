@@ -74,6 +74,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_status_string": (C.c_char_p, [_i]),
     "spx_abi_version": (_i, []),
     "spx_selftest_wait_timeout": (_i, [_vp]),
+    "spx_selftest_group_wait_timeout": (_i, [_vp]),
     "spx_next_pow2": (_u32, [_u32]),
     "spx_next_smooth23": (_u32, [_u32]),
     "spx_fft_size_supported": (_i, [_u32]),

@@ -24,6 +24,7 @@
 #pragma once
 
 #include <cooperative_groups.h>
+#include <cuda/atomic>
 
 #include "spx.h"
 #include "spx_device.cuh"
@@ -227,6 +228,29 @@ SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_
   const uintptr_t hi = (a + bytes) & ~(uintptr_t)127;
   for (uintptr_t x = lo + (uintptr_t)tid * 128; x < hi; x += (uintptr_t)T * 128)
     asm volatile("discard.global.L2 [%0], 128;" ::"l"(x) : "memory");
+}
+
+// Barrier of the C CTAs working on one beam (one cooperative launch, so all
+// CTAs are resident): every CTA adds one arrival to the beam's counter
+// (release) and waits until C have arrived (acquire), at most kSpinLimitNs,
+// then sets kErrLookbackTimeout and goes on.
+SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
+    r.fetch_add(1u, cuda::memory_order_release);
+    if (r.load(cuda::memory_order_acquire) < C) {
+      const uint64_t t0 = globaltimer_ns();
+      while (r.load(cuda::memory_order_acquire) < C) {
+        if (globaltimer_ns() - t0 > kSpinLimitNs) {
+          atomicOr(err, kErrLookbackTimeout);
+          break;
+        }
+      }
+    }
+  }
+  __syncthreads();
 }
 
 // Runs the passes p, p+1, ... while they have radix R; returns the next pass.

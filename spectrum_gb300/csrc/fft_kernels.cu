@@ -77,6 +77,46 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
   epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
 }
 
+// The same transform as fft_xl_kernel for power-of-two local sizes M (M / 16
+// threads) and C in {2, 4, 8, 16}, on all SMs: a persistent cooperative
+// launch of G groups of C CTAs (one CTA per SM for M = 16384), group q
+// transforming beams q, q + G, ...; a bounded device-memory barrier per beam
+// (group_barrier) replaces the cluster barrier (clusters of 8 one-SM CTAs fit
+// on 120 of the 152 SMs).
+template <int M>
+__global__ void __launch_bounds__(M / 16, 16384 / M)
+fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+                     FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
+                     float2* __restrict__ xch, uint32_t* __restrict__ arrive, uint32_t* __restrict__ err,
+                     uint32_t groups, void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  constexpr uint32_t T = M / 16;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t grp = blockIdx.x / g.C, c = blockIdx.x - grp * g.C;
+#pragma unroll 1
+  for (uint32_t beam = grp; beam < g.beams; beam += groups) {
+    float2* slot = xch + (size_t)beam * g.nfft;
+    const SampleLoader ld{in + (size_t)beam * n_point, n_point, win};
+    prefetch_future_beam(g, in, n_point, beam, c, tid, T);
+    switch (g.C) {
+      case 2: cross_stage_exchange<2>(slot, c, M, ld, tw_cross, tid, T); break;
+      case 4: cross_stage_exchange<4>(slot, c, M, ld, tw_cross, tid, T); break;
+      case 8: cross_stage_exchange<8>(slot, c, M, ld, tw_cross, tid, T); break;
+      default: cross_stage_exchange<16>(slot, c, M, ld, tw_cross, tid, T); break;
+    }
+    group_barrier(arrive + beam, g.C, err);
+    const float2* row = slot + (size_t)c * M;
+    p2_local_fft<M>(s, ExchangeLoader{row}, tw_local, tid);
+    discard_row_l2(row, (size_t)M * sizeof(float2), tid, T);
+    epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
+  }  // (the next beam's group barrier orders these reads of s before its local FFT)
+}
+
+bool group_geometry(const FftGeom& g) {
+  return g.C > 1 && (g.C & (g.C - 1)) == 0 && g.ept == 16 && (g.M == 4096 || g.M == 8192 || g.M == 16384) &&
+         g.T == g.M / 16;
+}
+
 // ---------------------------------------------------------------------------
 // Host: geometry and twiddle tables.
 // ---------------------------------------------------------------------------
@@ -352,10 +392,43 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_out_kernel");
     return SPX_OK;
   }
+  const size_t xch_bytes = ((size_t)beams * g.nfft * sizeof(float2) + 255) & ~(size_t)255;
   void* xch = nullptr;
-  spx_status st = get_scratch(ctx, kSlotExchange, (size_t)beams * g.nfft * sizeof(float2), &xch);
+  spx_status st = get_scratch(ctx, kSlotExchange, xch_bytes + (size_t)beams * sizeof(uint32_t), &xch);
   if (st != SPX_OK) return st;
   float2* xchp = static_cast<float2*>(xch);
+  if (group_geometry(g)) {
+    uint32_t* arrive = reinterpret_cast<uint32_t*>(static_cast<char*>(xch) + xch_bytes);
+    e = cudaMemsetAsync(arrive, 0, (size_t)beams * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(group barriers)");
+    const void* kfn = g.M == 16384 ? (const void*)fft_group_out_kernel<16384>
+                      : g.M == 8192 ? (const void*)fft_group_out_kernel<8192>
+                                    : (const void*)fft_group_out_kernel<4096>;
+    e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_group_out_kernel");
+    uint32_t groups = resident_ctas(kfn, g.T, smem, 1) / g.C;  // all resident at once (cooperative)
+    if (groups > beams) groups = beams;
+    if (groups == 0) return fail(ctx, SPX_ERR_CUDA, "fft_group_out_kernel: a group of CTAs does not fit the device");
+    g.beams = beams;
+    g.ahead = ctx->input_on_host ? 0u : groups;
+    uint32_t* err = ctx->d_error;
+    void* gargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
+                     (void*)&twc,  (void*)&xchp,    (void*)&arrive, (void*)&err,  (void*)&groups,
+                     (void*)&d_out, (void*)&out_mode, (void*)&scale};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(groups * g.C, 1, 1);
+    cfg.blockDim = dim3(g.T, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, kfn, gargs);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_group_out_kernel");
+    return SPX_OK;
+  }
   void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
                   (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};
   e = wide ? launch_beams(fft_xl_kernel<32>, g, beams, smem, ctx->stream, args, !ctx->input_on_host)

@@ -317,29 +317,6 @@ fft_peaks_kernel(FftGeom g, FusedArgs a) {
   write_window_row(row, s, g, c, a.start, a.end, tid, T);
 }
 
-// Barrier of the C CTAs working on one beam (one cooperative launch, so all
-// CTAs are resident): every CTA adds one arrival to the beam's counter
-// (release) and waits until C have arrived (acquire), at most kSpinLimitNs,
-// then sets kErrLookbackTimeout and goes on.
-SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
-    r.fetch_add(1u, cuda::memory_order_release);
-    if (r.load(cuda::memory_order_acquire) < C) {
-      const uint64_t t0 = globaltimer_ns();
-      while (r.load(cuda::memory_order_acquire) < C) {
-        if (globaltimer_ns() - t0 > kSpinLimitNs) {
-          atomicOr(err, kErrLookbackTimeout);
-          break;
-        }
-      }
-    }
-  }
-  __syncthreads();
-}
-
 // C > 1 with a power-of-two local size M (4096, 8192, 16384; M / 16 threads)
 // and C in {2, 4, 8, 16}: a persistent cooperative launch of G groups of C
 // CTAs (one CTA per SM); group q transforms beams q, q + G, ...  Per beam:
@@ -371,10 +348,18 @@ fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
   }
 }
 
-static bool group_supported(const FftGeom& g) {
-  return g.C > 1 && (g.C & (g.C - 1)) == 0 && g.ept == 16 && (g.M == 4096 || g.M == 8192 || g.M == 16384) &&
-         g.T == g.M / 16;
+// Self-test of the bounded wait: a single CTA arrives at a barrier that
+// expects two arrivals, so the wait ends at its time bound.
+__global__ void group_timeout_probe_kernel(uint32_t* count, uint32_t* err) { group_barrier(count, 2u, err); }
+
+spx_status launch_group_timeout_probe(spx_ctx* ctx, uint32_t* d_count) {
+  cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(uint32_t), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "group probe memset");
+  group_timeout_probe_kernel<<<1, 32, 0, ctx->stream>>>(d_count, ctx->d_error);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch group_timeout_probe_kernel");
 }
+
 
 // ---------------------------------------------------------------------------
 // maxima_cluster_kernel: every strict local maximum of |X| in [start, end)
@@ -716,7 +701,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   a.xch = static_cast<float2*>(p);
   uint32_t* ccount = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes);
   a.arrive = reinterpret_cast<uint32_t*>(static_cast<char*>(p) + xch_bytes + cnt_bytes);
-  if (group_supported(g)) {
+  if (group_geometry(g)) {
     e = cudaMemsetAsync(a.arrive, 0, (size_t)beams * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(group barriers)");
     const void* kfn = g.M == 16384 ? (const void*)fft_group_kernel<16384>

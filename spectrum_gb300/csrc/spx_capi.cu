@@ -190,6 +190,17 @@ spx_status spx_selftest_wait_timeout(spx_ctx* ctx) {
   return spx_synchronize(ctx);
 }
 
+spx_status spx_selftest_group_wait_timeout(spx_ctx* ctx) {
+  if (!ctx) return SPX_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  void* st = nullptr;
+  spx_status s = get_scratch(ctx, kSlotWork, sizeof(uint32_t), &st);
+  if (s != SPX_OK) return s;
+  s = launch_group_timeout_probe(ctx, static_cast<uint32_t*>(st));
+  if (s != SPX_OK) return s;
+  return spx_synchronize(ctx);
+}
+
 uint32_t spx_next_pow2(uint32_t n) {
   if (n == 0) return 1;
   n--;

@@ -5,6 +5,9 @@
 
 namespace spx {
 
+// Error word bits written by kernels into spx_ctx::d_error.
+constexpr uint32_t kErrLookbackTimeout = 1u;  // a bounded device-side wait gave up (look-back, beam group barrier)
+
 constexpr int kMaxPass = 12;
 constexpr uint32_t kMaxLocal = 16384;   // points per CTA (one local FFT)
 constexpr uint32_t kPrefLocalCluster = 16384;  // preferred points per CTA when C > 1 (measured fastest on GB300)

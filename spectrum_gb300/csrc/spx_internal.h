@@ -30,8 +30,6 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept = kEPTDefault,
                 uint32_t pref_local = kPrefLocalCluster);
 bool is_smooth23(uint32_t n);
 
-// Error word bits written by kernels into spx_ctx::d_error.
-constexpr uint32_t kErrLookbackTimeout = 1u;  // a bounded device-side wait gave up (look-back, beam group barrier)
 
 }  // namespace spx
 
@@ -96,6 +94,11 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
                             uint32_t* d_counts);
+// Geometries the persistent beam-group kernels take (power-of-two local size
+// M in {4096, 8192, 16384} with M/16 threads, C in {2, 4, 8, 16}).
+bool group_geometry(const FftGeom& g);
+// Self-test of the group barrier's bounded wait (one CTA, two arrivals expected).
+spx_status launch_group_timeout_probe(spx_ctx* ctx, uint32_t* d_count);
 // Longest search window maxima_cluster_kernel takes (8 CTAs x 32768 bins).
 constexpr uint32_t kMaxClusterSpan = 8u * 32768u;
 // All maxima of spectra whose bin k of beam b sits at

@@ -209,3 +209,29 @@ def test_bounded_wait_times_out_and_context_stays_usable(spx, cuda):
     out, counts = spx.all_maxima(torch.from_numpy(z).to(cuda), sample_rate=1.0)
     ref, rc = orc.all_maxima(None, z, 8192, 1.0)
     np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+
+
+def test_group_barrier_wait_times_out_and_context_stays_usable(spx, cuda):
+    """The per-beam group barrier of the large fused transform gives up after
+    its 1 s bound when an arrival never comes: SPX_ERR_TIMEOUT, then the same
+    context runs the large fused search (which uses that barrier) correctly."""
+    import time
+
+    import torch
+    from spectrum_gb300 import synth
+    ctx = spx.default_context()
+    ctx.bind_stream()
+    t0 = time.perf_counter()
+    st = spx.lib.spx_selftest_group_wait_timeout(ctx.h)
+    dt = time.perf_counter() - t0
+    assert st == spx._capi.SPX_ERR_TIMEOUT
+    assert 0.9 < dt < 30.0
+    assert spx.lib.spx_synchronize(ctx.h) == spx._capi.SPX_OK
+    bs = synth.make_beams([65536] * 3, tones=(1, 8), snr_db=(10.0, 40.0), seed=5)
+    x = synth.synth_numpy(bs)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, 131072, window=spx.WINDOW_HANN).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, 131072, spx.WINDOW_HANN, spx.PEAK_ALL, sample_rate=1.0, thresh_sigma=6.0)
+    ref, rc = orc.all_maxima(None, spec, 131072, 1.0, thresh_sigma=6.0)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    np.testing.assert_array_equal(spx.maxvalues_to_numpy(out)[0, :int(rc[0])]["index"], ref[0, :int(rc[0])]["index"])
