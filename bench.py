@@ -36,9 +36,9 @@ BEAMS, N_POINT, NFFT = 256, 65536, 131072
 FS = 1.0
 SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
-# DRAM bytes (read + write) of one step on this workload (fft_peaks_kernel +
-# maxima_cluster_kernel), from an ncu capture (profiles/fft_peaks_kernel_plain_large.md).
-NCU_TRAFFIC_BYTES = 359_455_744
+# DRAM bytes (read + write) of one step on this workload (fft_group_kernel +
+# maxima_cluster_kernel), from an ncu capture (profiles/fft_group_kernel_plain_large.md).
+NCU_TRAFFIC_BYTES = 359_430_912
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
@@ -383,17 +383,18 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
     # algorithmic bytes: samples read once + maxima and counts written
     algo = BEAMS * N_POINT * 8 + n_max * 32 + BEAMS * 4
     return {
-        "path": "spx_fft_peaks: fft_peaks_kernel (one cluster of 8 CTAs x 1024 threads per beam: window, "
-                "zero pad, 131072-point FFT; the search window's bins in row layout into the beam's L2 "
-                "exchange slot) then maxima_cluster_kernel (one cluster of 8 CTAs x 256 threads per beam, "
-                "5 CTAs per SM: |X|, noise histogram merged through DSMEM, 6-sigma threshold, maxima, ranks)",
+        "path": "spx_fft_peaks: fft_group_kernel<16384> (persistent cooperative launch, 19 groups of 8 CTAs x "
+                "1024 threads, one CTA per SM; per beam: window, zero pad, 131072-point FFT with a device-memory "
+                "group barrier, the search window's bins in row layout into the beam's L2 exchange slot) then "
+                "maxima_cluster_kernel (one cluster of 8 CTAs x 256 threads per beam, 5 CTAs per SM: |X|, noise "
+                "histogram merged through DSMEM, 6-sigma threshold, maxima, ranks)",
         "components_ms": {"fused_step": round(f, 4), "composed_fft_complex": round(statistics.median(fft_ms), 4),
                           "composed_peaks": round(statistics.median(peak_ms), 4)},
-        "roofline": {"bound": "hbm", "kernel": "fft_peaks_kernel + maxima_cluster_kernel (one step)",
+        "roofline": {"bound": "hbm", "kernel": "fft_group_kernel + maxima_cluster_kernel (one step)",
                      "achieved": round(algo / (f * 1e-3) / 1e9, 1),
                      "unit": "GB/s", "traffic": NCU_TRAFFIC_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of each "
-                                       "kernel (profiles/fft_peaks_kernel_plain_large.md)",
+                                       "kernel (profiles/fft_group_kernel_plain_large.md)",
                      "algorithmic_bytes_per_launch": algo,
                      "maxima_per_launch": n_max},
         "launches_per_step": 2,
