@@ -132,6 +132,8 @@ def test_fused_large_workload_properties(spx, cuda):
 
 @pytest.mark.parametrize("nfft,n_point,beams,mode,k,sigma,pinned", [
     (131072, 65536, 70, "all", 1000, 6.0, True),    # 3 chunks of 32 beams (last partial)
+    (131072, 65536, 137, "all", 1000, 6.0, True),   # more beams than resident beam groups
+    (65536, 60000, 250, "all", 1000, 3.0, True),    # groups of 4 CTAs
     (4096, 4096, 2600, "topk", 5, 0.0, True),      # 6 chunks: input and output slots reused
     (4096, 4000, 1100, "one", 0, 0.0, False),      # pageable numpy input, ONE_PEAK (no counts)
 ])
