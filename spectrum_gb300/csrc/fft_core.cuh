@@ -231,15 +231,22 @@ SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_
 }
 
 // Barrier of the C CTAs working on one beam (one cooperative launch, so all
-// CTAs are resident): every CTA adds one arrival to the beam's counter
-// (release) and waits until C have arrived (acquire), at most kSpinLimitNs,
-// then sets kErrLookbackTimeout and goes on.
-SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
+// CTAs are resident), in two halves so that a CTA can work between them:
+// group_arrive adds this CTA's arrival to the beam's counter (release, after
+// every thread's prior writes); group_wait waits until C have arrived
+// (acquire), at most kSpinLimitNs, then sets kErrLookbackTimeout and goes on.
+SPX_DEV void group_arrive(uint32_t* count) {
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
     r.fetch_add(1u, cuda::memory_order_release);
+  }
+}
+
+SPX_DEV void group_wait(uint32_t* count, uint32_t C, uint32_t* err) {
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
     if (r.load(cuda::memory_order_acquire) < C) {
       const uint64_t t0 = globaltimer_ns();
       while (r.load(cuda::memory_order_acquire) < C) {
@@ -251,6 +258,11 @@ SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
     }
   }
   __syncthreads();
+}
+
+SPX_DEV void group_barrier(uint32_t* count, uint32_t C, uint32_t* err) {
+  group_arrive(count);
+  group_wait(count, C, err);
 }
 
 // Runs the passes p, p+1, ... while they have radix R; returns the next pass.

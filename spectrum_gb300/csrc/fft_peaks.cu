@@ -330,8 +330,8 @@ fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
   constexpr uint32_t T = M / 16;
   const uint32_t tid = threadIdx.x;
   const uint32_t grp = blockIdx.x / g.C, c = blockIdx.x - grp * g.C;
-#pragma unroll 1
-  for (uint32_t beam = grp; beam < g.beams; beam += groups) {
+  // cross stage of a beam into its exchange slot, then this CTA's arrival
+  auto cross = [&](uint32_t beam) {
     float2* slot = a.xch + (size_t)beam * g.nfft;
     const SampleLoader ld{a.in + (size_t)beam * a.n_point, a.n_point, a.win};
     prefetch_future_beam(g, a.in, a.n_point, beam, c, tid, T);
@@ -341,8 +341,17 @@ fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
       case 8: cross_stage_exchange<8>(slot, c, M, ld, a.tw_cross, tid, T); break;
       default: cross_stage_exchange<16>(slot, c, M, ld, a.tw_cross, tid, T); break;
     }
-    group_barrier(a.arrive + beam, g.C, a.err);
-    float2* row = slot + (size_t)c * M;
+    group_arrive(a.arrive + beam);
+  };
+  // The cross stage of the group's next beam runs between the arrival and
+  // the wait of the current one: a CTA that waits for its group's slowest
+  // member does so with the next beam's samples already exchanged.
+  if (grp < g.beams) cross(grp);
+#pragma unroll 1
+  for (uint32_t beam = grp; beam < g.beams; beam += groups) {
+    if (beam + groups < g.beams) cross(beam + groups);
+    group_wait(a.arrive + beam, g.C, a.err);
+    float2* row = a.xch + (size_t)beam * g.nfft + (size_t)c * M;
     p2_local_fft<M>(s, ExchangeLoader{row}, a.tw_local, tid);
     write_window_row(row, s, g, c, a.start, a.end, tid, T);
   }
