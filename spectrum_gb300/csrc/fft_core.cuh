@@ -167,6 +167,7 @@ SPX_DEV void cross_stage_exchange(float2* __restrict__ slot, uint32_t c, uint32_
   const uint32_t S = (M + CR - 1) / CR;
   const uint32_t lo = c * S;
   const uint32_t hi = min(lo + S, M);
+#pragma unroll 2
   for (uint32_t n2 = lo + tid; n2 < hi; n2 += T) {
     float2 v[CR];
 #pragma unroll
