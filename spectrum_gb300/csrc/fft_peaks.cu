@@ -455,8 +455,31 @@ maxima_cluster_kernel(MxArgs a) {
   //    are in flight to cover the device-memory latency)
   uint32_t bmin = kHist, bmax = 0;
   if (nb && tid < 2) smag[tid ? nb + 1 : 0] = mag_rn(mx_load(a, sb, tid ? hi : lo - 1));  // neighbours
+  auto take = [&](uint32_t i, float2 z) {  // |X| of bin lo + i into shared memory and the histogram
+    const float m = mag_rn(z);
+    smag[i + 1] = m;
+    if (thr_on) {
+      const uint32_t b = bucket_of(m);
+      atomicAdd(&hist[b >> 1], 1u << ((b & 1u) * 16));
+      bmin = min(bmin, b);
+      bmax = max(bmax, b);
+    }
+  };
+  // Power-of-two C1 divides kMxThreads: the kMxBatch bins lo + i0 + j*256 + tid
+  // of a full batch lie in one row, 256 / C1 columns apart.
+  const bool rows_fixed = a.c1shift < 32;
   for (uint32_t i0 = 0; i0 < nb; i0 += kMxBatch * kMxThreads) {
     float2 z[kMxBatch];
+    if (rows_fixed && i0 + kMxBatch * kMxThreads <= nb) {
+      const uint32_t k = lo + i0 + tid;
+      const float2* p = sb + ((k & (a.C1 - 1)) * a.M1 + (k >> a.c1shift));
+      const uint32_t step = kMxThreads >> a.c1shift;
+#pragma unroll
+      for (uint32_t j = 0; j < kMxBatch; ++j) z[j] = __ldcs(p + j * step);
+#pragma unroll
+      for (uint32_t j = 0; j < kMxBatch; ++j) take(i0 + j * kMxThreads + tid, z[j]);
+      continue;
+    }
 #pragma unroll
     for (uint32_t j = 0; j < kMxBatch; ++j) {
       const uint32_t i = i0 + j * kMxThreads + tid;
@@ -465,16 +488,7 @@ maxima_cluster_kernel(MxArgs a) {
 #pragma unroll
     for (uint32_t j = 0; j < kMxBatch; ++j) {
       const uint32_t i = i0 + j * kMxThreads + tid;
-      if (i < nb) {
-        const float m = mag_rn(z[j]);
-        smag[i + 1] = m;
-        if (thr_on) {
-          const uint32_t b = bucket_of(m);
-          atomicAdd(&hist[b >> 1], 1u << ((b & 1u) * 16));
-          bmin = min(bmin, b);
-          bmax = max(bmax, b);
-        }
-      }
+      if (i < nb) take(i, z[j]);
     }
   }
   float thr = -INFINITY;
