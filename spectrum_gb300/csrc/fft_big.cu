@@ -54,7 +54,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
   for (int a = 1; a < J; ++a) {
     const uint32_t e = (t * a) % CB;
-    v[a] = cmul(v[a], __ldg(twN + (uint64_t)e * (nfft / CB)));  // W_CB^{e} = W_N^{e N/CB}
+    v[a] = cmul(v[a], __ldg(twN + e * kBigM));  // W_CB^{e} = W_N^{e N/CB}, N/CB = kBigM
   }
   __syncthreads();
 #pragma unroll
@@ -71,8 +71,8 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
       const uint32_t k1 = t + J * b;
-      const uint64_t m = ((uint64_t)n2 * k1) % nfft;
-      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + m));
+      // W_N^{n2 k1}: n2 < kBigM and k1 < CB, so n2 * k1 < kBigM * CB = nfft (no reduction)
+      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + n2 * k1));
     }
   }
 }

@@ -79,6 +79,8 @@ ALL_CASES = [
     (4096, 2, 5, 4096, 50, "ties"),        # end >= nfft -> nfft - 1
     (4096, 2, 3000, 100, 1000, "noise"),   # empty window (end < start)
     (2048, 1, 1, 3, 1000, "noise"),        # tiny window
+    (524288, 1, 0, 262145, 1000, "noise"),  # 262144 bins: the longest window of the cluster kernel
+    (1 << 20, 1, 0, (1 << 20) - 1, 1000, "noise"),  # longer: the look-back kernel
 ]
 
 
@@ -124,6 +126,17 @@ def test_all_maxima_threshold_and_refine(spx, cuda, refine, sigma):
         assert_maxvalues_equal(got[b], ref[b], n=int(rcounts[b]))
     if sigma == 6.0:  # planted lines inside [1, nfft/2) survive, noise maxima do not
         assert (rcounts >= 1).all() and (rcounts < 20).all()
+
+
+@pytest.mark.parametrize("nfft,end", [(524288, 262145), (1 << 20, (1 << 20) - 1)])
+def test_all_maxima_threshold_at_window_limits(spx, cuda, nfft, end):
+    """Thresholded search at 262144 bins (cluster kernel, 32768 bins per CTA)
+    and beyond (histogram/select kernels + look-back kernel): oracle lists."""
+    z = _noise_spectrum(1, nfft, 5, tones=30)
+    out, counts = spx.all_maxima(_dev(z, cuda), None, 1000.0, 1, end, 1000, 1, 3.0)
+    ref, rcounts = orc.all_maxima(None, z, nfft, 1000.0, 1, end, 1000, 1, 3.0)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rcounts)
+    assert_maxvalues_equal(spx.maxvalues_to_numpy(out)[0], ref[0], n=min(int(rcounts[0]), ref.shape[1]))
 
 
 # ---- TOP-K -----------------------------------------------------------------------
