@@ -736,7 +736,9 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
     uint32_t groups = resident_ctas(kfn, g.T, smem, 1) / g.C;
     if (groups > beams) groups = beams;
     if (groups == 0) return fail(ctx, SPX_ERR_CUDA, "fft_group_kernel: a group of CTAs does not fit the device");
-    g.ahead = ctx->input_on_host ? 0u : groups;
+    // prefetch distance: one round of the groups (also for samples in host
+    // memory, which then cross the host link while the current beams compute)
+    g.ahead = groups;
     void* args[] = {(void*)&g, (void*)&a, (void*)&groups};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(groups * g.C, 1, 1);
