@@ -259,10 +259,13 @@ spx_status spx_all_maxima_noalloc(spx_ctx* ctx, const float* d_mag, const void* 
                                   spx_max_value* d_out, uint32_t* d_counts);
 
 /* ---- fused: raw samples -> peaks ---------------------------------------- */
-/* Window + zero-pad + FFT + |X| + peak search in one pass; the spectrum never
- * goes to device memory.  params->mode selects ONE/TWO/ALL/TOPK with the
- * layouts of spx_peaks_one_two / spx_all_maxima / spx_topk.  d_counts may be
- * NULL for ONE/TWO. */
+/* Window + zero-pad + FFT + |X| + peak search.  nfft <= 16384 (ALL, TOPK):
+ * one launch, the spectrum never goes to device memory.  ALL with nfft >
+ * 16384: the FFT writes only the search window's bins (device scratch), then
+ * one maxima launch.  Other cases: spx_fft, then the peak function.
+ * params->mode selects ONE/TWO/ALL/TOPK with the layouts of
+ * spx_peaks_one_two / spx_all_maxima / spx_topk.  d_counts may be NULL for
+ * ONE/TWO; d_out may be NULL for ALL when the capacity is 0. */
 spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
                          uint32_t n_point, uint32_t nfft, uint32_t window,
                          const spx_peak_params* params, spx_max_value* d_out,
@@ -275,7 +278,8 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
  * 117-119; src/fft_func/src/spectrum_processor_rocm.cpp:444-500).  h_in holds
  * beams x n_point complex64; h_out receives beams x R MaxValue (R = 4 ONE,
  * 8 TWO, the spx_all_maxima_capacity for ALL, K for TOPK) and h_counts the
- * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO).  Page-locked,
+ * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO; h_out may be NULL when
+ * R is 0).  Page-locked,
  * device-mapped input (cudaHostAlloc; cudaHostRegister with mapping) is read
  * by the kernel in place over the host link; other input goes through in
  * ~16 MiB chunks whose upload, transform and read-back overlap on three

@@ -65,7 +65,7 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
   if (params->mode > SPX_PEAK_TOPK)
     return fail(ctx, SPX_ERR_INVALID_ARG, "unknown peak mode " + std::to_string(params->mode));
   if (beams == 0) return SPX_OK;
-  if (!h_in || !h_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: null host pointer");
+  if (!h_in) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: null host pointer");
   if (n_point == 0 || nfft < n_point)
     return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: need 0 < n_point <= nfft");
   const bool counted = params->mode == SPX_PEAK_ALL || params->mode == SPX_PEAK_TOPK;
@@ -82,6 +82,8 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
     }
     default: per = params->max_per_beam; break;
   }
+  // the output may be null only when it has no rows (ALL with a zero capacity)
+  if (!h_out && per > 0) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: null host pointer");
   DeviceGuard guard(ctx->device);
   // Page-locked, device-mapped input: the kernel reads it over the host link
   // itself (the link carries ~210 GB/s either way; reading in place has no
@@ -116,8 +118,9 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
                         reinterpret_cast<spx_max_value*>(o), counted ? c : nullptr);
     ctx->input_on_host = false;
     if (st0 != SPX_OK) return st0;
-    cudaError_t e0 = cudaMemcpyAsync(h_out, o, (size_t)beams * per * sizeof(spx_max_value), cudaMemcpyDeviceToHost,
-                                     ctx->stream);
+    cudaError_t e0 = per == 0 ? cudaSuccess
+                              : cudaMemcpyAsync(h_out, o, (size_t)beams * per * sizeof(spx_max_value),
+                                                cudaMemcpyDeviceToHost, ctx->stream);
     if (e0 == cudaSuccess && counted)
       e0 = cudaMemcpyAsync(h_counts, c, (size_t)beams * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "spx_fft_peaks_host: read-back");
@@ -163,7 +166,7 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
     }
     e = cudaEventRecord(ev_comp[i], ctx->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_out, ev_comp[i], 0);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && per > 0)
       e = cudaMemcpyAsync(h_out + (size_t)b0 * per, o, (size_t)nb * per * sizeof(spx_max_value),
                           cudaMemcpyDeviceToHost, ctx->copy_out);
     if (e == cudaSuccess && counted)

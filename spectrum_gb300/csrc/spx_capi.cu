@@ -419,9 +419,16 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
   if (params->mode > SPX_PEAK_TOPK)
     return fail(ctx, SPX_ERR_INVALID_ARG, "unknown peak mode " + std::to_string(params->mode));
   if (beams == 0) return SPX_OK;
-  if (!d_in || !d_out) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: null device pointer");
+  if (!d_in) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: null device pointer");
   if (n_point == 0 || nfft < n_point)
     return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: need 0 < n_point <= nfft");
+  // the output may be null only for ALL with a zero capacity (nothing is written, as in spx_all_maxima)
+  if (!d_out) {
+    uint32_t s0 = 0, e0 = 0, cap0 = 1;
+    if (params->mode == SPX_PEAK_ALL)
+      spx_all_maxima_capacity(nfft, params->search_start, params->search_end, params->max_per_beam, &s0, &e0, &cap0);
+    if (cap0 > 0) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks: null device pointer");
+  }
   DeviceGuard g(ctx->device);
   const FftPlan* plan = nullptr;
   spx_status st = get_plan(ctx, nfft, &plan);

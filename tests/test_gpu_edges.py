@@ -138,3 +138,31 @@ def test_argument_errors_are_invalid_argument(spx, cuda):
         spx.all_maxima(x, thresh_sigma=-1.0)
     with pytest.raises(ValueError):
         spx.fft_peaks(x, 64, mode=7)
+
+
+@pytest.mark.parametrize("nfft,n_point,start,end,sigma", [
+    (131072, 65536, 1, 2, 0.0),              # one bin
+    (131072, 65536, 65535, 65536, 0.0),      # one bin at the default end
+    (131072, 65536, 131060, 131071, 0.0),    # last bins; end = nfft - 1
+    (131072, 65536, 100, 300, 1.0),          # narrower than one CTA's share of the maxima kernel
+    (131072, 100000, 7, 200000, 2.0),        # end beyond nfft: clipped to nfft - 1
+    (65536, 65536, 3, 65533, 0.5),           # groups of 4 CTAs, many maxima above the threshold
+    (39366, 39000, 11, 39360, 6.0),          # 3-smooth size (cluster path), wide window
+])
+def test_large_fused_search_window_edges(spx, cuda, nfft, n_point, start, end, sigma):
+    """spx_fft_peaks for nfft > 16384 (the FFT writes only the window's bins,
+    then the maxima kernel): counts and records equal to the oracle on the
+    spectrum spx_fft returns, for windows at the ends and of every width."""
+    import torch
+    x = _rand(2, n_point, nfft + start)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_ALL, sample_rate=1.0, refine=1,
+                                thresh_sigma=sigma, search_start=start, search_end=end)
+    ref, rc = orc.all_maxima(None, spec, nfft, 1.0, start, end, refine=1, thresh_sigma=sigma)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    got = spx.maxvalues_to_numpy(out)
+    for b in range(2):
+        n = min(int(rc[b]), ref.shape[1])
+        for f in ["index", "real", "imag", "magnitude", "freq_offset", "refined_frequency"]:
+            np.testing.assert_array_equal(got[b, :n][f], ref[b, :n][f], err_msg=f"beam {b} field {f}")
