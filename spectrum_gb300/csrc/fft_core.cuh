@@ -233,13 +233,15 @@ SPX_DEV void discard_row_l2(const float2* p, size_t bytes, uint32_t tid, uint32_
 
 // Barrier of the C CTAs working on one beam (one cooperative launch, so all
 // CTAs are resident), in two halves so that a CTA can work between them:
-// group_arrive adds this CTA's arrival to the beam's counter (release, after
-// every thread's prior writes); group_wait waits until C have arrived
-// (acquire), at most kSpinLimitNs, then sets kErrLookbackTimeout and goes on.
+// group_arrive adds this CTA's arrival to the beam's counter; group_wait
+// waits until C have arrived (acquire), at most kSpinLimitNs, then sets
+// kErrLookbackTimeout and goes on.  As in a grid-wide barrier, the CTA
+// barrier orders every thread's prior writes before thread 0's device-scope
+// fence and release, so only thread 0 fences.
 SPX_DEV void group_arrive(uint32_t* count) {
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     cuda::atomic_ref<uint32_t, cuda::thread_scope_device> r(*count);
     r.fetch_add(1u, cuda::memory_order_release);
   }
