@@ -21,7 +21,8 @@ namespace spx {
 
 constexpr uint32_t kBigM = 16384;
 
-// One tile = 32 consecutive n2 columns x Cb rows (n1), 8 threads per column.
+// One tile = 32 consecutive n2 columns x Cb rows (n1); lane = column, warp
+// t = row group (tile reads conflict-free, output rows written 256 bytes at a time).
 template <int CB>
 __global__ void __launch_bounds__(256)
 big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
@@ -44,7 +45,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
     tile[n1][col] = load_sample(x, n1 * kBigM + n2_0 + col, n_point, win);
   }
   __syncthreads();
-  const uint32_t col = tid >> 3, t = tid & 7;
+  const uint32_t col = tid & 31, t = tid >> 5;
   constexpr int J = CB / 8;  // stage-1 radix (8 or 4)
   // stage 1: thread t transforms rows t + 8j (j < J), twiddles W_CB^{t a}
   float2 v[J];
