@@ -403,6 +403,36 @@ constexpr uint32_t kOutComplexReversed = 16;  // out[(nfft - k) mod nfft] = X[k]
 constexpr uint32_t kOutR2CHalf = 17;          // k <= nfft/2: out[beam (nfft/2 + 1) + k] = X[k]
 constexpr uint32_t kOutR2CFull = 18;          // k <= nfft/2: X[k] at k, conj(X[k]) at nfft - k
 
+// Writes bin k (= X[k]) of one beam in output mode `out_mode` (the layouts of
+// epilogue_out below).
+SPX_DEV void store_bin(void* __restrict__ out, uint32_t out_mode, float scale, const FftGeom& g,
+                       uint32_t beam, uint32_t k, float2 z) {
+  const size_t obase = (size_t)beam * g.nfft;
+  const uint32_t half = g.nfft / 2;
+  switch (out_mode) {
+    case SPX_OUT_COMPLEX: reinterpret_cast<float2*>(out)[obase + k] = z; break;
+    case SPX_OUT_MAG: reinterpret_cast<float*>(out)[obase + k] = __fmul_rn(mag_rn(z), scale); break;
+    case SPX_OUT_MAG2: reinterpret_cast<float*>(out)[obase + k] = __fmul_rn(mag2_rn(z), scale); break;
+    case SPX_OUT_MAGPHASE:
+      reinterpret_cast<float2*>(out)[obase + k] = make_float2(mag_rn(z), atan2f(z.y, z.x));
+      break;
+    case kOutComplexReversed:
+      reinterpret_cast<float2*>(out)[obase + (k == 0 ? 0u : g.nfft - k)] =
+          make_float2(__fmul_rn(z.x, scale), __fmul_rn(z.y, scale));
+      break;
+    case kOutR2CHalf:
+      if (k <= half) reinterpret_cast<float2*>(out)[(size_t)beam * (half + 1) + k] = z;
+      break;
+    default:  // kOutR2CFull
+      if (k <= half) {
+        float2* o = reinterpret_cast<float2*>(out) + obase;
+        o[k] = z;
+        if (k >= 1 && k < g.nfft - half) o[g.nfft - k] = make_float2(z.x, -z.y);
+      }
+      break;
+  }
+}
+
 // Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
 SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
                           void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
