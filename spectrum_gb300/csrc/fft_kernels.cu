@@ -82,13 +82,16 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
 // launch of G groups of C CTAs (one CTA per SM for M = 16384), group q
 // transforming beams q, q + G, ...; a bounded device-memory barrier per beam
 // (group_barrier) replaces the cluster barrier (clusters of 8 one-SM CTAs fit
-// on 120 of the 152 SMs).
+// on 120 of the 152 SMs).  Each CTA leaves its spectrum row in the beam's
+// exchange slot; rows_transpose_kernel then writes the output (the stride-C
+// stores of a direct epilogue cost more than the extra pass: 0.332 vs 0.313 ms
+// for 256 x 131072 points).
 template <int M>
 __global__ void __launch_bounds__(M / 16, 16384 / M)
 fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
                      FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
                      float2* __restrict__ xch, uint32_t* __restrict__ arrive, uint32_t* __restrict__ err,
-                     uint32_t groups, void* __restrict__ out, uint32_t out_mode, float scale) {
+                     uint32_t groups) {
   extern __shared__ float2 s[];
   constexpr uint32_t T = M / 16;
   const uint32_t tid = threadIdx.x;
@@ -105,11 +108,49 @@ fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
       default: cross_stage_exchange<16>(slot, c, M, ld, tw_cross, tid, T); break;
     }
     group_barrier(arrive + beam, g.C, err);
-    const float2* row = slot + (size_t)c * M;
+    float2* row = slot + (size_t)c * M;
     p2_local_fft<M>(s, ExchangeLoader{row}, tw_local, tid);
-    discard_row_l2(row, (size_t)M * sizeof(float2), tid, T);
-    epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
+    // row c was read by this CTA alone: it takes the CTA's spectrum row
+    // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
+    for (uint32_t i = tid; i < M; i += T) __stcg(row + i, s[sw(i)]);
   }  // (the next beam's group barrier orders these reads of s before its local FFT)
+}
+
+// Bins k1 + C*q of the output from the row layout rows[beam][k1][q] (C rows
+// of M columns per beam, C <= 64): one CTA per `tc` columns of one beam; the
+// tile comes in along the rows (contiguous runs) and goes out in bin order
+// (contiguous runs in every output mode but the mirrored ones), through
+// shared memory with a row pitch of tc + 1 (conflict-free both ways).
+__global__ void __launch_bounds__(256)
+rows_transpose_kernel(FftGeom g, const float2* __restrict__ rows, uint32_t tc, uint32_t cmagic,
+                      void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 tile[];  // [C][tc + 1]
+  const uint32_t tid = threadIdx.x, C = g.C, M = g.M, ld = tc + 1;
+  const uint32_t beam = blockIdx.y, q0 = blockIdx.x * tc;
+  const uint32_t tshift = 31u - __clz(tc);  // tc is a power of two
+  const float2* src = rows + (size_t)beam * g.nfft + q0;
+  for (uint32_t f = tid; f < C * tc; f += 256) {
+    const uint32_t r = f >> tshift, q = f & (tc - 1);
+    if (q0 + q < M) tile[r * ld + q] = __ldcs(src + (size_t)r * M + q);
+  }
+  __syncthreads();
+  const uint32_t k0 = C * q0;
+  for (uint32_t e = tid; e < C * tc; e += 256) {
+    const uint32_t q = __umulhi(e, cmagic), k1 = e - q * C;  // e div C, e mod C
+    if (q0 + q < M) store_bin(out, out_mode, scale, g, beam, k0 + e, tile[k1 * ld + q]);
+  }
+}
+
+spx_status launch_rows_transpose(spx_ctx* ctx, const FftGeom& g, const float2* rows, uint32_t beams,
+                                 void* d_out, uint32_t out_mode, float scale) {
+  uint32_t tc = 32;
+  while (g.C * tc < 1024) tc *= 2;
+  const uint32_t cmagic = 0xFFFFFFFFu / g.C + 1u;  // e div C = umulhi(e, cmagic) for e * C < 2^32
+  const size_t smem = (size_t)g.C * (tc + 1) * sizeof(float2);
+  const dim3 grid((g.M + tc - 1) / tc, beams);
+  rows_transpose_kernel<<<grid, 256, smem, ctx->stream>>>(g, rows, tc, cmagic, d_out, out_mode, scale);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch rows_transpose_kernel");
 }
 
 bool group_geometry(const FftGeom& g) {
@@ -412,9 +453,8 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     g.beams = beams;
     g.ahead = ctx->input_on_host ? 0u : groups;
     uint32_t* err = ctx->d_error;
-    void* gargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
-                     (void*)&twc,  (void*)&xchp,    (void*)&arrive, (void*)&err,  (void*)&groups,
-                     (void*)&d_out, (void*)&out_mode, (void*)&scale};
+    void* gargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,   (void*)&twl,
+                     (void*)&twc,  (void*)&xchp,    (void*)&arrive, (void*)&err, (void*)&groups};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(groups * g.C, 1, 1);
     cfg.blockDim = dim3(g.T, 1, 1);
@@ -427,7 +467,7 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     cfg.numAttrs = 1;
     e = cudaLaunchKernelExC(&cfg, kfn, gargs);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_group_out_kernel");
-    return SPX_OK;
+    return launch_rows_transpose(ctx, g, xchp, beams, d_out, out_mode, scale);
   }
   void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
                   (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};

@@ -94,6 +94,10 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
                             uint32_t* d_counts);
+// Output of C spectrum rows per beam (rows[beam][k1][q] = X[k1 + C*q], the
+// exchange-slot layout) to bin order in any output mode (fft_kernels.cu).
+spx_status launch_rows_transpose(spx_ctx* ctx, const FftGeom& g, const float2* rows, uint32_t beams,
+                                 void* d_out, uint32_t out_mode, float scale);
 // Geometries the persistent beam-group kernels take (power-of-two local size
 // M in {4096, 8192, 16384} with M/16 threads, C in {2, 4, 8, 16}).
 bool group_geometry(const FftGeom& g);
