@@ -8,11 +8,10 @@
 //   launch 2 (big_rows_kernel): for each (beam, k1), the M-point Stockham FFT
 //     of row k1 (the passes of fft_core.cuh), X[k1 + Cb*k2] written back over
 //     the row it read (scratch[beam][k1][k2], one coalesced pass);
-//   launch 3 (big_transpose_kernel): scratch[beam][k1][k2] -> bin k1 + Cb*k2
-//     of the output in the requested mode, 32 x Cb tiles through shared
-//     memory, so the output is written in contiguous runs (written straight
-//     from launch 2, the stride-Cb stores kept its SMs waiting on the store
-//     queue: 0.63 ms for 64 x 2^20 points).
+//   launch 3 (rows_transpose_kernel, fft_kernels.cu): scratch[beam][k1][k2]
+//     -> bin k1 + Cb*k2 of the output in the requested mode, written in
+//     contiguous runs (written straight from launch 2, the stride-Cb stores
+//     kept its SMs waiting on the store queue: 0.63 ms for 64 x 2^20 points).
 // All twiddles are FP64-generated and stored in FP32 (W_N^m from one table of
 // nfft entries, W_M from the local plan), which is what the 120 dB dynamic
 // range of the precision workload needs.  Replaces hipFFT's internal
@@ -98,26 +97,6 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, float2* __restri
   for (uint32_t i = tid; i < g.M; i += T) __stcs(row + i, s[sw(i)]);
 }
 
-// Bins k1 + Cb*k2 of the output from scratch[beam][k1][k2]: one CTA per 32
-// columns k2 of one beam; lane = column on the way in (256-byte row runs),
-// consecutive threads on consecutive bins on the way out.
-template <int CB>
-__global__ void __launch_bounds__(256)
-big_transpose_kernel(FftGeom g, const float2* __restrict__ scratch, void* __restrict__ out,
-                     uint32_t out_mode, float scale) {
-  __shared__ float2 tile[CB][33];
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t beam = blockIdx.y, k2_0 = blockIdx.x * 32;
-  const float2* src = scratch + (size_t)beam * g.nfft + k2_0 + lane;
-#pragma unroll
-  for (uint32_t r = warp; r < (uint32_t)CB; r += 8) tile[r][lane] = __ldcs(src + (size_t)r * kBigM);
-  __syncthreads();
-  const uint32_t k0 = CB * k2_0;
-#pragma unroll
-  for (uint32_t e = tid; e < (uint32_t)CB * 32; e += 256)
-    store_bin(out, out_mode, scale, g, beam, k0 + e, tile[e % CB][e / CB]);
-}
-
 bool big_size(uint32_t nfft) { return nfft == (1u << 19) || nfft == (1u << 20); }
 
 // Geometry of the row FFTs (M = 16384, C = Cb as the output stride) and the
@@ -182,14 +161,7 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   void* args[] = {(void*)&gg, (void*)&twl, (void*)&scratch};
   e = cudaLaunchKernel(kfn, dim3(beams * g.C), dim3(g.T), args, (size_t)g.Mpad * sizeof(float2), ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_rows_kernel");
-  const dim3 tgrid(kBigM / 32, beams);
-  if (g.C == 64)
-    big_transpose_kernel<64><<<tgrid, 256, 0, ctx->stream>>>(g, scratch, d_out, out_mode, scale);
-  else
-    big_transpose_kernel<32><<<tgrid, 256, 0, ctx->stream>>>(g, scratch, d_out, out_mode, scale);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_transpose_kernel");
-  return SPX_OK;
+  return launch_rows_transpose(ctx, g, scratch, beams, d_out, out_mode, scale);
 }
 
 }  // namespace spx

@@ -51,7 +51,7 @@ template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
               FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ tw_cross,
-              float2* __restrict__ xch, void* __restrict__ out, uint32_t out_mode, float scale) {
+              float2* __restrict__ xch) {
   extern __shared__ float2 s[];
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t tid = threadIdx.x, T = blockDim.x;
@@ -71,10 +71,11 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
     default: cross_stage_exchange<16>(slot, c, g.M, ld, tw_cross, tid, T); break;
   }
   cl.sync();
-  const float2* row = slot + (size_t)c * g.M;
+  float2* row = slot + (size_t)c * g.M;
   local_fft<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T);
-  discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
-  epilogue_out(s, g, c, beam, out, out_mode, scale, tid, T);
+  // row c was read by this CTA alone: it takes the CTA's spectrum row
+  // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
+  for (uint32_t i = tid; i < g.M; i += T) __stcg(row + i, s[sw(i)]);
 }
 
 // The same transform as fft_xl_kernel for power-of-two local sizes M (M / 16
@@ -469,12 +470,12 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_group_out_kernel");
     return launch_rows_transpose(ctx, g, xchp, beams, d_out, out_mode, scale);
   }
-  void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,     (void*)&twl,
-                  (void*)&twc,  (void*)&xchp,    (void*)&d_out, (void*)&out_mode, (void*)&scale};
+  void* args[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&g,
+                  (void*)&twl,  (void*)&twc,     (void*)&xchp};
   e = wide ? launch_beams(fft_xl_kernel<32>, g, beams, smem, ctx->stream, args, !ctx->input_on_host)
            : launch_beams(fft_xl_kernel<16>, g, beams, smem, ctx->stream, args, !ctx->input_on_host);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_xl_kernel");
-  return SPX_OK;
+  return launch_rows_transpose(ctx, g, xchp, beams, d_out, out_mode, scale);
 }
 
 }  // namespace spx
