@@ -8,9 +8,12 @@
 //      launch.  The launch has fixed cluster dims Cl (the largest per-beam
 //      cluster size); each cluster hosts one or several beams on disjoint
 //      rank ranges (first-fit decreasing packing), beams needing no cluster
-//      run on single CTAs.  Spectra go to a packed buffer.
+//      run on single CTAs.  Each CTA leaves its spectrum row in the beam's
+//      exchange slot (row c: X[c + C*i] at column i; one row for C = 1):
+//      stores in contiguous runs instead of stride-C scatter.
 //   2. topk_batch_kernel: the K largest strict local maxima of every beam,
-//      one CTA per beam, the same selection rules as spx_topk.
+//      one CTA per beam, the same selection rules as spx_topk, reading bin k
+//      from row k mod C of the beam's slot.
 // The "plain" path runs the same two kernels once per distinct nfft (one
 // plan per size, as a per-size library call would), so its results are
 // bit-identical to the batched run by construction.
@@ -33,7 +36,7 @@ constexpr uint32_t kIdle = 0xFFFFFFFFu;
 
 struct BatchBeam {
   uint64_t in_off;    // first sample in the packed input (complex elements)
-  uint64_t spec_off;  // first bin in the packed spectra / exchange slots
+  uint64_t spec_off;  // first element of the beam's exchange slot (its spectrum rows after the FFT)
   uint32_t n_point, nfft, geom, pad;
 };
 struct BatchCta {
@@ -100,8 +103,7 @@ template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ beams,
                  const BatchCta* __restrict__ ctas, const BatchGeom* __restrict__ geoms,
-                 uint32_t window, float2* __restrict__ xch, float2* __restrict__ spec,
-                 uint32_t ahead) {
+                 uint32_t window, float2* __restrict__ xch, uint32_t ahead) {
   extern __shared__ float2 s[];
   cg::cluster_group cl = cg::this_cluster();
   const uint32_t tid = threadIdx.x, T = blockDim.x;
@@ -138,16 +140,14 @@ fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ be
   }
   cl.sync();  // every CTA of the cluster exactly once
   if (!active) return;
+  float2* row = slot + (size_t)d.c * g.M;  // read by this CTA alone (C > 1)
   if (g.C == 1) {
     first_pass_dispatch<EPT>(s, g, ld, tid, T);
   } else {
-    const float2* row = slot + (size_t)d.c * g.M;
     first_pass_dispatch<EPT>(s, g, ExchangeLoader{row}, tid, T);
-    discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
   }
   local_passes<EPT>(s, g, 1, twl, tid, T);
-  float2* o = spec + bm.spec_off + d.c;
-  for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = s[sw(i)];
+  for (uint32_t i = tid; i < g.M; i += T) row[i] = s[sw(i)];
 }
 
 // Top-K strict local maxima of every beam's spectrum (one CTA per beam),
@@ -161,9 +161,9 @@ SPX_DEV uint64_t bt_insert(uint64_t mine, uint64_t x, uint32_t lane) {
 }
 
 __global__ void __launch_bounds__(kBtThreads)
-topk_batch_kernel(const float2* __restrict__ spec, const BatchBeam* __restrict__ beams,
-                  const uint32_t* __restrict__ beam_list, uint32_t K, uint32_t start0,
-                  uint32_t end0, float fs, uint32_t refine, MaxValueDev* __restrict__ out,
+topk_batch_kernel(const float2* __restrict__ xch, const BatchBeam* __restrict__ beams,
+                  const BatchGeom* __restrict__ geoms, const uint32_t* __restrict__ beam_list, uint32_t K,
+                  uint32_t start0, uint32_t end0, float fs, uint32_t refine, MaxValueDev* __restrict__ out,
                   uint32_t* __restrict__ counts) {
   __shared__ uint64_t lists[kBtThreads / 32][32];
   const uint32_t beam = beam_list ? beam_list[blockIdx.x] : blockIdx.x;
@@ -171,7 +171,15 @@ topk_batch_kernel(const float2* __restrict__ spec, const BatchBeam* __restrict__
   const uint32_t nfft = bm.nfft;
   uint32_t start = start0 == 0 ? 1 : start0, end = end0 == 0 ? nfft / 2 : end0;
   if (end >= nfft) end = nfft - 1;
-  const float2* f = spec + bm.spec_off;
+  // bin k of the beam: row k mod C, column k div C of its slot
+  const uint32_t C = geoms[bm.geom].g.C, M = geoms[bm.geom].g.M;
+  const uint32_t cmagic = 0xFFFFFFFFu / C + 1u;  // k div C = umulhi(k, cmagic) (k * C < 2^32)
+  const float2* fs_row = xch + bm.spec_off;
+  auto bin = [&](uint32_t k) -> float2 {
+    if (C == 1) return __ldg(fs_row + k);
+    const uint32_t q = __umulhi(k, cmagic);
+    return __ldg(fs_row + (size_t)(k - q * C) * M + q);
+  };
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t mine = 0;
   for (uint32_t base = start + warp * 32; base < end; base += kBtThreads) {
@@ -179,8 +187,8 @@ topk_batch_kernel(const float2* __restrict__ spec, const BatchBeam* __restrict__
     uint64_t key = 0;
     bool cand = false;
     if (k < end) {
-      const float c = mag_rn(__ldg(f + k));
-      cand = (c > mag_rn(__ldg(f + k - 1))) && (c > mag_rn(__ldg(f + k + 1)));
+      const float c = mag_rn(bin(k));
+      cand = (c > mag_rn(bin(k - 1))) && (c > mag_rn(bin(k + 1)));
       key = ((uint64_t)__float_as_uint(c) << 32) | (uint32_t)(~k);
     }
     const uint64_t kth = __shfl_sync(0xffffffffu, mine, K - 1);
@@ -206,7 +214,7 @@ topk_batch_kernel(const float2* __restrict__ spec, const BatchBeam* __restrict__
     const uint32_t k = ~(uint32_t)mine;
     const float bw = __fdiv_rn(fs, (float)nfft);
     const float yc = __uint_as_float((uint32_t)(mine >> 32));
-    const float yl = mag_rn(f[k - 1]), yr = mag_rn(f[k + 1]);
+    const float yl = mag_rn(bin(k - 1)), yr = mag_rn(bin(k + 1));
     float fo = 0.f, rf = __fmul_rn((float)k, bw);
     if (refine == SPX_REFINE_PARABOLIC) {
       const float denom = __fadd_rn(__fsub_rn(yl, __fmul_rn(2.0f, yc)), yr);
@@ -217,7 +225,7 @@ topk_batch_kernel(const float2* __restrict__ spec, const BatchBeam* __restrict__
         rf = __fmul_rn(__fadd_rn((float)k, fo), bw);
       }
     }
-    const float2 z = f[k];
+    const float2 z = bin(k);
     out[(size_t)beam * K + lane] =
         MaxValueDev{k, z.x, z.y, yc, __fmul_rn(atan2f(z.y, z.x), kRadToDeg), fo, rf, 0u};
   }
@@ -247,7 +255,6 @@ struct spx_batch {
   BatchBeam* d_beams = nullptr;
   BatchGeom* d_geoms = nullptr;
   float2* d_xch = nullptr;
-  float2* d_spec = nullptr;
   uint32_t ept = kEPTDefault, points_per_cta = kPrefLocalCluster;
   LaunchSet all;                       // the single batched launch
   std::vector<LaunchSet> per_size;     // the per-size ("plain") launches
@@ -378,10 +385,9 @@ spx_status launch_set(spx_ctx* ctx, spx_batch* b, const LaunchSet& ls, const voi
   const BatchGeom* geoms = b->d_geoms;
   uint32_t window = b->window;
   float2* xch = b->d_xch;
-  float2* spec = b->d_spec;
   uint32_t ahead = resident_ctas(kfn, ls.threads, ls.smem, ls.cluster);
   void* args[] = {(void*)&in, (void*)&beams, (void*)&ctas, (void*)&geoms,
-                  (void*)&window, (void*)&xch, (void*)&spec, (void*)&ahead};
+                  (void*)&window, (void*)&xch, (void*)&ahead};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(ls.n_ctas, 1, 1);
   cfg.blockDim = dim3(ls.threads, 1, 1);
@@ -397,7 +403,7 @@ spx_status launch_set(spx_ctx* ctx, spx_batch* b, const LaunchSet& ls, const voi
   e = cudaLaunchKernelExC(&cfg, kfn, args);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch fft_batch_kernel");
   topk_batch_kernel<<<ls.n_beams, kBtThreads, 0, ctx->stream>>>(
-      b->d_spec, b->d_beams, ls.d_beam_list, b->K, b->start, b->end, b->fs, b->refine,
+      b->d_xch, b->d_beams, b->d_geoms, ls.d_beam_list, b->K, b->start, b->end, b->fs, b->refine,
       reinterpret_cast<MaxValueDev*>(d_out), d_counts);
   e = cudaGetLastError();
   return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch topk_batch_kernel");
@@ -459,12 +465,8 @@ spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_poin
   spx_status st = build_launches(ctx, b);
   if (st == SPX_OK) {
     cudaError_t e = cudaMalloc(&b->d_xch, b->spec_total * sizeof(float2));
-    if (e == cudaSuccess) {
-      b->allocs.push_back(b->d_xch);
-      e = cudaMalloc(&b->d_spec, b->spec_total * sizeof(float2));
-      if (e == cudaSuccess) b->allocs.push_back(b->d_spec);
-    }
-    if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMalloc(batch spectra)");
+    if (e == cudaSuccess) b->allocs.push_back(b->d_xch);
+    if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMalloc(batch exchange slots)");
   }
   if (st != SPX_OK) {
     delete b;
