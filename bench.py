@@ -53,14 +53,15 @@ def _parse():
                     help="skip the small / uneven / precision / learned workload timings")
     ap.add_argument("--profile", action="store_true",
                     help="device steps only (warmup + steps), no timing report; for ncu captures")
-    ap.add_argument("--profile-workload", default="large", choices=["large", "plain4096", "plain16384", "uneven"],
+    ap.add_argument("--profile-workload", default="large",
+                    choices=["large", "plain4096", "plain16384", "uneven", "precision"],
                     help="with --profile: the fused large step, the plain FFT (|X|^2 out) of 16384 x 4096 or "
-                         "2048 x 16384 points, or the uneven batch")
+                         "2048 x 16384 points, the uneven batch, or the 64 x 2^20 Blackman-Harris FFT")
     return ap.parse_args()
 
 
 def run_profile_other(args):
-    """--profile steps of the plain FFT or the uneven batch (for ncu)."""
+    """--profile steps of the plain FFT, the uneven batch or the precision FFT (for ncu)."""
     import ctypes as C
 
     import torch
@@ -77,6 +78,13 @@ def run_profile_other(args):
         b = Batch(bs.lengths, window=spx.WINDOW_HANN, k=8, sample_rate=1.0, ctx=ctx)
         for _ in range(args.warmup + args.steps):
             b.run(x)
+    elif args.profile_workload == "precision":
+        bp = synth.workload_precision(seed=3, beams=64)
+        x = synth.synth_torch(bp, device=dev)
+        o = torch.empty((64, 1 << 20), dtype=torch.complex64, device=dev)
+        for _ in range(args.warmup + args.steps):
+            ctx.check(spx.lib.spx_fft(ctx.h, C.c_void_p(x.data_ptr()), 64, 1 << 20, 1 << 20,
+                                      spx.WINDOW_BLACKMAN_HARRIS, spx.OUT_COMPLEX, 1.0, C.c_void_p(o.data_ptr())))
     else:
         n = 4096 if args.profile_workload == "plain4096" else 16384
         beams = (1 << 26) // n
