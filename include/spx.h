@@ -28,8 +28,8 @@
  *                              src/fft_func/src/all_maxima_pipeline_rocm.cpp:258-472)
  *   spx_topk               -> (no reference counterpart: top-K of local maxima)
  *   spx_fft_peaks          -> ISpectrumProcessor::ProcessFromGPU / FindAllMaximaFromGPUPipeline
- *                             fused into one launch (include/spectrum/interface/
- *                             i_spectrum_processor.hpp:95-129)
+ *                             fused: one launch up to nfft 16384, FFT + maxima launch
+ *                             above (include/spectrum/interface/i_spectrum_processor.hpp:95-129)
  */
 #ifndef SPX_H_
 #define SPX_H_

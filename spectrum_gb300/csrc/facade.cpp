@@ -257,7 +257,7 @@ std::vector<FFTMagPhaseResult> FFTProcessorGB300::ProcessMagPhase(void* gpu_data
 
 // FFTProcessorROCm::ProcessMagnitudesToGPU (fft_processor_rocm.cpp:585-659):
 // window + pad + FFT + |X| (or |X|^2) with inv_n = 1 into the caller buffer;
-// here in one fused launch.
+// here spx_fft with its |X| epilogue (no separate pad or magnitude pass).
 void FFTProcessorGB300::ProcessMagnitudesToGPU(void* gpu_data, void* gpu_out_magnitudes,
                                                const FFTProcessorParams& params, bool squared, WindowType window,
                                                ROCmProfEvents* prof_events) {
@@ -575,8 +575,9 @@ void SpectrumProcessorGB300::ReallocateBuffersForBatch(size_t batch_antenna_coun
   out_.ensure(batch_antenna_count * 8 * sizeof(MaxValue), "ReallocateBuffersForBatch");
 }
 
-// ONE_PEAK / TWO_PEAKS on beams already in device memory: one fused launch
-// (pad + FFT + post kernel), then ReadResults (spectrum_processor_rocm.cpp:1072-1122).
+// ONE_PEAK / TWO_PEAKS on beams already in device memory: spx_fft_peaks
+// (windowed, zero-padded FFT, then the post kernel), then ReadResults
+// (spectrum_processor_rocm.cpp:1072-1122).
 std::vector<SpectrumResult> SpectrumProcessorGB300::peaks_from_device(const void* d_in, size_t beams,
                                                                       size_t start_antenna) {
   if (params_.peak_mode == PeakSearchMode::ALL_MAXIMA)

@@ -434,8 +434,8 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
   spx_status st = get_plan(ctx, nfft, &plan);
   if (st != SPX_OK) return st;
   // Fused path: ALL maxima and TOP-K in one launch for C == 1 (the spectrum
-  // stays on chip); ALL maxima for C > 1 as the cluster FFT, which writes the
-  // window's bins, and the maxima cluster kernel.
+  // stays on chip); ALL maxima for C > 1 as the beam-group (or cluster) FFT,
+  // which writes only the window's bins, and the maxima cluster kernel.
   if (params->mode == SPX_PEAK_ALL || params->mode == SPX_PEAK_TOPK) {
     st = peak_common_checks(ctx, params, nfft);
     if (st != SPX_OK) return st;
