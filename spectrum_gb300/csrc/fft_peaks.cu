@@ -544,18 +544,27 @@ maxima_cluster_kernel(MxArgs a) {
   } else {
     __syncthreads();
   }
-  // 3. bins lo + u*256 + warp*32 + lane -> bit lane of word u*8 + warp
+  // 3. a thread tests 4 consecutive bins i = 4*(u*256 + tid) .. +3 from one
+  //    16-byte and one 8-byte load of |X| (bin i is smag[i + 1]); the 8
+  //    lanes of a group of 32 bins merge their 4-bit pieces into the word.
   const uint32_t words = (nb + 31) / 32;
-  for (uint32_t u = 0; u * kMxThreads < nb; ++u) {
-    const uint32_t i = u * kMxThreads + tid;
-    bool f = false;
-    if (i < nb) {
-      const float v = smag[i + 1];
-      f = (v > smag[i]) && (v > smag[i + 2]) && (v > thr);
+  for (uint32_t u = 0; u * 4 * kMxThreads < nb; ++u) {
+    const uint32_t i = 4 * (u * kMxThreads + tid);
+    uint32_t piece = 0;
+    if (i < nb) {  // smag[i .. i + 5]: i + 5 <= chunk + 1, inside the array
+      const float4 m4 = *reinterpret_cast<const float4*>(smag + i);
+      const float2 m2 = *reinterpret_cast<const float2*>(smag + i + 4);
+      const float m[6] = {m4.x, m4.y, m4.z, m4.w, m2.x, m2.y};
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (i + j < nb && m[j + 1] > m[j] && m[j + 1] > m[j + 2] && m[j + 1] > thr) piece |= 1u << j;
     }
-    const uint32_t b = __ballot_sync(0xffffffffu, f);
-    const uint32_t w = u * (kMxThreads / 32) + warp;
-    if (lane == 0 && w < words) bits[w] = b;
+    uint32_t word = piece << (4 * (lane & 7));
+    word |= __shfl_xor_sync(0xffffffffu, word, 1);
+    word |= __shfl_xor_sync(0xffffffffu, word, 2);
+    word |= __shfl_xor_sync(0xffffffffu, word, 4);
+    const uint32_t w = u * (4 * kMxThreads / 32) + warp * 4 + (lane >> 3);
+    if ((lane & 7) == 0 && w < words) bits[w] = word;
   }
   __syncthreads();
   // contiguous words per thread, block-wide exclusive scan of their maxima
