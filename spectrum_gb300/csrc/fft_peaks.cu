@@ -391,7 +391,7 @@ constexpr uint32_t kMxThreads = 256;
 constexpr uint32_t kMxMinBlocks = 5;  // CTAs per SM the kernel is built for (<= 48 registers)
 constexpr uint32_t kMxMaxC2 = 8;
 constexpr uint32_t kMxMaxChunk = 32768;  // < 65536: 16-bit histogram counters cannot overflow
-constexpr uint32_t kMxBatch = 8;         // loads in flight per thread
+constexpr uint32_t kMxBatch = 4;         // loads in flight per thread (8 and 16 measured slower)
 static_assert(kMxMaxC2 * kMxMaxChunk == kMaxClusterSpan, "window limit of spx_all_maxima");
 constexpr uint32_t kMxMerge = 512;       // buckets of the merged histogram per window
 
