@@ -209,3 +209,39 @@ def test_fused_exact_ties(spx, cuda, nfft, sigma):
         ref, rc = orc.topk(None, spec, nfft, 1.0, 8, thresh_sigma=sigma)
         np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
         assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+
+
+def test_concurrent_large_searches_on_two_streams(spx, cuda):
+    """Two contexts on two streams run the large search (cooperative beam-group
+    FFT + maxima kernel) at the same time, repeatedly: every result equals the
+    serial result and no bounded wait gives up (spx_synchronize is SPX_OK)."""
+    import torch
+    from spectrum_gb300 import Context
+    x = torch.from_numpy(_beams(96, 65536, 17)).to(cuda)
+    y = torch.from_numpy(_beams(96, 65536, 18)).to(cuda)
+    kw = dict(sample_rate=1.0, refine=1, thresh_sigma=6.0)
+    ref_x = [t.clone() for t in spx.fft_peaks(x, 131072, spx.WINDOW_HANN, spx.PEAK_ALL, **kw)]
+    ref_y = [t.clone() for t in spx.fft_peaks(y, 131072, spx.WINDOW_HANN, spx.PEAK_ALL, **kw)]
+    torch.cuda.synchronize()
+    ca, cb = Context(0), Context(0)
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    results = []
+    for _ in range(8):
+        with torch.cuda.stream(sa):
+            ra = spx.fft_peaks(x, 131072, spx.WINDOW_HANN, spx.PEAK_ALL, ctx=ca, **kw)
+        with torch.cuda.stream(sb):
+            rb = spx.fft_peaks(y, 131072, spx.WINDOW_HANN, spx.PEAK_ALL, ctx=cb, **kw)
+        results.append((ra, rb))
+    torch.cuda.synchronize()
+    for c, s in ((ca, sa), (cb, sb)):
+        c.bind_stream(s)
+        assert spx.lib.spx_synchronize(c.h) == 0
+    for ra, rb in results:
+        for got, ref in ((ra, ref_x), (rb, ref_y)):
+            assert torch.equal(got[1], ref[1])
+            g0, r0, cnt = got[0].cpu(), ref[0].cpu(), ref[1].cpu()
+            for b in range(cnt.shape[0]):
+                n = min(int(cnt[b]), r0.shape[1])  # rows past a beam's count are not written
+                assert torch.equal(g0[b, :n], r0[b, :n])
+    ca.close()
+    cb.close()
