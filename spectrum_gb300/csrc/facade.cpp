@@ -193,7 +193,8 @@ std::vector<R> FFTProcessorGB300::run(const std::complex<float>* host, void* gpu
       const float* src = raw.data() + i * (size_t)nfft * 2;
       if constexpr (is_complex_result<R>()) {
         r.spectrum.resize(nfft);
-        std::memcpy(r.spectrum.data(), src, (size_t)nfft * 8);
+        // std::complex<float> has the layout of float[2] (array-oriented access)
+        std::memcpy(static_cast<void*>(r.spectrum.data()), src, (size_t)nfft * 8);
       } else {
         r.magnitude.resize(nfft);
         r.phase.resize(nfft);
