@@ -564,9 +564,11 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
 def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
     """End to end through the C ABI's host-buffer entry point
     (spx_fft_peaks_host): page-locked host samples in, host maxima and counts
-    out; the upload, the fused kernel and the read-back of ~16 MiB chunks
-    overlap on three streams.  Timed with the host clock around whole calls
-    (each call returns with the results in host memory)."""
+    out.  The 128 MiB of samples go up in 16 MiB chunks on a copy stream, each
+    overlapping the previous chunk's transform and search, whose kernel writes
+    the maxima and counts into the page-locked outputs in place.  Timed with
+    the host clock around whole calls (each call returns with the results in
+    host memory)."""
     import ctypes as C
 
     import torch
@@ -596,7 +598,8 @@ def time_e2e(spx, ctx, x_dev, out, counts, p, stream, args):
     return {"value": round(BEAMS * N_POINT / (ms * 1e-3) / 1e6, 2), "unit": "Msamples/s",
             "ms_per_step": round(ms, 4), "h2d_bytes_per_step": int(host_in.numel() * 8),
             "d2h_bytes_per_step": int(host_out.numel() * 4 + host_cnt.numel() * 4),
-            "api": "spx_fft_peaks_host (page-locked host buffers read and written in place over the host link)",
+            "api": "spx_fft_peaks_host (page-locked host buffers: samples uploaded in 16 MiB chunks "
+                   "overlapping the compute, maxima written in place over the host link)",
             "counts_match_device_path": same}
 
 

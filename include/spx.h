@@ -280,10 +280,13 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams,
  * 8 TWO, the spx_all_maxima_capacity for ALL, K for TOPK) and h_counts the
  * per-beam counts (ALL/TOPK; may be NULL for ONE/TWO; h_out may be NULL when
  * R is 0).  Page-locked,
- * device-mapped input (cudaHostAlloc; cudaHostRegister with mapping) is read
- * by the kernel in place over the host link; other input goes through in
- * ~16 MiB chunks whose upload, transform and read-back overlap on three
- * streams.  Returns after the results are in host memory. */
+ * device-mapped input (cudaHostAlloc; cudaHostRegister with mapping) of at
+ * most 112 MiB is read by the kernel in place over the host link; larger or
+ * pageable input goes through in ~16 MiB chunks whose upload overlaps the
+ * previous chunk's transform and search.  Page-locked, mapped outputs are
+ * written by the kernel in place; others are copied back (per chunk, on a
+ * third stream, when chunked).  Returns after the results are in host
+ * memory. */
 spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
                               uint32_t n_point, uint32_t nfft, uint32_t window,
                               const spx_peak_params* params, spx_max_value* h_out,

@@ -3,21 +3,34 @@
 // FindAllMaximaFromCPU (src/fft_func/src/spectrum_processor_rocm.cpp:444-500:
 // upload, FFT, peak search, read back).
 //
+// The host link carries ~210 GB/s whichever engine drives it (copy engines
+// on one or several streams, or a kernel reading page-locked memory), so the
+// upload of the samples sets the floor and the question is how much of the
+// transform and the search hides behind it.
+//
 // Page-locked input that the device can address (cudaHostAlloc, or
-// cudaHostRegister with mapping) is read by the kernel in place over the
-// host link; the peaks are written in place too when the output buffers are
-// mapped, else they come back in one copy.  Other input goes through in
-// chunks of about kChunkBytes of samples on three streams: copy-in (host ->
-// device), the context's stream (the fused spx_fft_peaks launch) and
-// copy-out (device -> host), so the upload of chunk
-// i + 1 overlaps the transform of chunk i and the read-back of chunk i - 1.
-// Staging: three input slots and two output slots in one device buffer owned
-// by the context.  Events order slot reuse:
+// cudaHostRegister with mapping) of at most kZeroCopyMaxBytes is read by the
+// kernel in place over the host link: no pipeline fill or drain, but the
+// maxima kernel of every beam runs after the last sample has arrived.
+//
+// Larger input, and pageable input, goes through in chunks of about
+// kChunkBytes of samples on the copy-in stream (host -> device) and the
+// context's stream (the fused spx_fft_peaks launch), so the upload of chunk
+// i + 1 overlaps the transform and search of chunk i and only the last
+// chunk's compute is exposed.  The peaks are written by the kernel straight
+// into mapped output buffers; other output comes back per chunk on the
+// copy-out stream.  Staging: three input slots (and, for copied-back output,
+// two output slots) in one device buffer owned by the context.  Events order
+// slot reuse:
 //   copy-in of chunk i waits until chunk i - 3 was computed (its input slot);
 //   compute of chunk i waits for its upload and for the read-back of chunk
 //   i - 2 (its output slot).
 // With pageable host memory the chunk copies are still correct but do not
 // overlap.
+//
+// Measured on the all-maxima search of 65536-point beams (nFFT 131072):
+// 128 beams (64 MiB) 0.415 ms in place vs 0.454 ms chunked; 256 beams
+// (128 MiB) 0.770 vs 0.740 ms; 512 beams (256 MiB) 1.472 vs 1.396 ms.
 #include <algorithm>
 #include <cstring>
 
@@ -28,6 +41,7 @@ using namespace spx;
 namespace {
 
 constexpr size_t kChunkBytes = size_t(16) << 20;
+constexpr size_t kZeroCopyMaxBytes = 7 * kChunkBytes;
 constexpr int kInSlots = 3, kOutSlots = 2;
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -85,9 +99,6 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
   // the output may be null only when it has no rows (ALL with a zero capacity)
   if (!h_out && per > 0) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_fft_peaks_host: null host pointer");
   DeviceGuard guard(ctx->device);
-  // Page-locked, device-mapped input: the kernel reads it over the host link
-  // itself (the link carries ~210 GB/s either way; reading in place has no
-  // pipeline fill or drain), results come back in one copy.
   auto device_view = [](const void* p) -> void* {
     cudaPointerAttributes a{};
     const bool ok = p && cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
@@ -96,10 +107,13 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
   };
   cudaPointerAttributes pa{};
   pa.devicePointer = device_view(h_in);
-  const bool mapped = pa.devicePointer != nullptr;
-  void* dv_out = mapped ? device_view(h_out) : nullptr;
-  void* dv_cnt = mapped && counted ? device_view(h_counts) : nullptr;
-  if (mapped && dv_out && (!counted || dv_cnt)) {  // everything in place
+  const size_t beam_in = (size_t)n_point * sizeof(float2);
+  // mapped input up to kZeroCopyMaxBytes: the kernel reads it over the host link
+  const bool zero_copy = pa.devicePointer != nullptr && (size_t)beams * beam_in <= kZeroCopyMaxBytes;
+  void* dv_out = device_view(h_out);
+  void* dv_cnt = counted ? device_view(h_counts) : nullptr;
+  const bool out_in_place = dv_out && (!counted || dv_cnt);
+  if (zero_copy && out_in_place) {  // everything in place
     ctx->input_on_host = true;
     spx_status st0 = spx_fft_peaks(ctx, pa.devicePointer, beams, n_point, nfft, window, params,
                                    static_cast<spx_max_value*>(dv_out), static_cast<uint32_t*>(dv_cnt));
@@ -107,7 +121,7 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
     if (st0 != SPX_OK) return st0;
     return spx_synchronize(ctx);
   }
-  if (mapped) {
+  if (zero_copy) {  // results come back in one copy
     const size_t out_bytes = align_up((size_t)beams * std::max<uint32_t>(per, 1) * sizeof(spx_max_value), 256);
     spx_status st0 = ensure_pipeline(ctx, out_bytes + (size_t)beams * sizeof(uint32_t), 0);
     if (st0 != SPX_OK) return st0;
@@ -126,13 +140,12 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
     if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "spx_fft_peaks_host: read-back");
     return spx_synchronize(ctx);
   }
-  const size_t beam_in = (size_t)n_point * sizeof(float2);
   const uint32_t cb = (uint32_t)std::max<size_t>(1, std::min<size_t>(beams, kChunkBytes / beam_in));
   const uint32_t nchunks = (beams + cb - 1) / cb;
   const size_t in_slot = align_up((size_t)cb * beam_in, 256);
   const size_t out_slot = align_up((size_t)cb * std::max<uint32_t>(per, 1) * sizeof(spx_max_value), 256);
   const size_t cnt_slot = align_up((size_t)cb * sizeof(uint32_t), 256);
-  const size_t total = kInSlots * in_slot + kOutSlots * (out_slot + cnt_slot);
+  const size_t total = kInSlots * in_slot + (out_in_place ? 0 : kOutSlots * (out_slot + cnt_slot));
   spx_status st = ensure_pipeline(ctx, total, (size_t)3 * nchunks);
   if (st != SPX_OK) return st;
   char* base = static_cast<char*>(ctx->d_stage);
@@ -154,10 +167,18 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
                           ctx->copy_in);
     if (e == cudaSuccess) e = cudaEventRecord(ev_in[i], ctx->copy_in);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ev_in[i], 0);
-    if (e == cudaSuccess && i >= (uint32_t)kOutSlots) e = cudaStreamWaitEvent(ctx->stream, ev_out[i - kOutSlots], 0);
+    if (e == cudaSuccess && !out_in_place && i >= (uint32_t)kOutSlots)
+      e = cudaStreamWaitEvent(ctx->stream, ev_out[i - kOutSlots], 0);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: upload");
-    char* o = out_ptr(i);
-    uint32_t* c = reinterpret_cast<uint32_t*>(o + out_slot);
+    char* o = nullptr;
+    uint32_t* c = nullptr;
+    if (out_in_place) {  // the kernel writes this chunk's rows into the mapped output
+      o = reinterpret_cast<char*>(static_cast<spx_max_value*>(dv_out) + (size_t)b0 * per);
+      if (counted) c = static_cast<uint32_t*>(dv_cnt) + b0;
+    } else {
+      o = out_ptr(i);
+      c = reinterpret_cast<uint32_t*>(o + out_slot);
+    }
     st = spx_fft_peaks(ctx, in_ptr(i), nb, n_point, nfft, window, params, reinterpret_cast<spx_max_value*>(o),
                        counted ? c : nullptr);
     if (st != SPX_OK) {
@@ -165,7 +186,9 @@ extern "C" spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_
       return st;
     }
     e = cudaEventRecord(ev_comp[i], ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_out, ev_comp[i], 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "spx_fft_peaks_host: ordering");
+    if (out_in_place) continue;
+    e = cudaStreamWaitEvent(ctx->copy_out, ev_comp[i], 0);
     if (e == cudaSuccess && per > 0)
       e = cudaMemcpyAsync(h_out + (size_t)b0 * per, o, (size_t)nb * per * sizeof(spx_max_value),
                           cudaMemcpyDeviceToHost, ctx->copy_out);

@@ -131,15 +131,18 @@ def test_fused_large_workload_properties(spx, cuda):
 
 
 @pytest.mark.parametrize("nfft,n_point,beams,mode,k,sigma,pinned", [
-    (131072, 65536, 70, "all", 1000, 6.0, True),    # 3 chunks of 32 beams (last partial)
+    (131072, 65536, 70, "all", 1000, 6.0, True),    # 35 MiB mapped: read in place
     (131072, 65536, 137, "all", 1000, 6.0, True),   # more beams than resident beam groups
-    (65536, 60000, 250, "all", 1000, 3.0, True),    # groups of 4 CTAs
-    (4096, 4096, 2600, "topk", 5, 0.0, True),      # 6 chunks: input and output slots reused
+    (65536, 60000, 250, "all", 1000, 3.0, True),    # 114 MiB: 8 uploaded chunks, groups of 4 CTAs
+    (4096, 4096, 4100, "topk", 5, 0.0, True),      # 128 MiB: 9 chunks, input and output slots reused
+    (4096, 4096, 1300, "topk", 5, 0.0, True),      # 40 MiB mapped: read in place
     (4096, 4000, 1100, "one", 0, 0.0, False),      # pageable numpy input, ONE_PEAK (no counts)
 ])
 def test_fft_peaks_host_matches_device_path(spx, cuda, nfft, n_point, beams, mode, k, sigma, pinned):
-    """spx_fft_peaks_host (host in, host out, chunked copy/compute overlap)
-    returns exactly what spx_fft_peaks returns on the same samples."""
+    """spx_fft_peaks_host (host in, host out; mapped input read in place or,
+    above 112 MiB, uploaded in chunks that overlap the compute) returns
+    exactly what spx_fft_peaks returns on the same samples, with the peaks
+    copied back or written in place into page-locked outputs."""
     import torch
     from spectrum_gb300 import synth
     bs = synth.make_beams([n_point] * beams, tones=(1, 8), snr_db=(0.0, 40.0), seed=nfft + beams)
