@@ -460,6 +460,12 @@ spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_poin
       return fail(ctx, SPX_ERR_INVALID_ARG,
                   "spx_batch_create: beam " + std::to_string(i) + " has an unsupported size");
     }
+    if (big_size(n)) {  // three-launch transforms: not a cluster of the batch kernel
+      delete b;
+      return fail(ctx, SPX_ERR_UNSUPPORTED,
+                  "spx_batch_create: beam " + std::to_string(i) + " needs nfft " + std::to_string(n) +
+                      "; 2^19 and 2^20 points run through spx_fft_peaks, not in a batch");
+    }
     b->nfft[i] = n;
   }
   spx_status st = build_launches(ctx, b);

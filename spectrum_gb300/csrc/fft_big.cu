@@ -12,9 +12,10 @@
 //     -> bin k1 + Cb*k2 of the output in the requested mode, written in
 //     contiguous runs (written straight from launch 2, the stride-Cb stores
 //     kept its SMs waiting on the store queue: 0.63 ms for 64 x 2^20 points).
-// All twiddles are FP64-generated and stored in FP32 (W_N^m from one table of
-// nfft entries, W_M from the local plan), which is what the 120 dB dynamic
-// range of the precision workload needs.  Replaces hipFFT's internal
+// All twiddles are FP64-generated and stored in FP32 (W_N^{n2 k1} in a table
+// of nfft entries laid out [k1][n2], so a warp's 32 columns read 256
+// contiguous bytes; W_M from the local plan), which is what the 120 dB
+// dynamic range of the precision workload needs.  Replaces hipFFT's internal
 // multi-pass plan for large sizes (src/fft_func/src/fft_processor_rocm.cpp:176-193).
 #include <cmath>
 #include <vector>
@@ -60,7 +61,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
   for (int a = 1; a < J; ++a) {
     const uint32_t e = (t * a) % CB;
-    v[a] = cmul(v[a], __ldg(twN + e * kBigM));  // W_CB^{e} = W_N^{e N/CB}, N/CB = kBigM
+    v[a] = cmul(v[a], __ldg(twN + nfft + e));  // W_CB^e, after the [k1][n2] table
   }
   __syncthreads();
 #pragma unroll
@@ -77,8 +78,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
       const uint32_t k1 = t + J * b;
-      // W_N^{n2 k1}: n2 < kBigM and k1 < CB, so n2 * k1 < kBigM * CB = nfft (no reduction)
-      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + n2 * k1));
+      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + (size_t)k1 * kBigM + n2));  // W_N^{n2 k1}
     }
   }
 }
@@ -118,11 +118,17 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
         twl[gl.twoff[p] + (r - 1) * Ns + k] = make_float2((float)std::cos(a), (float)std::sin(a));
       }
   }
-  std::vector<float2> twn(nfft);
-  for (uint32_t m = 0; m < nfft; ++m) {
+  // [k1][n2] = W_N^{n2 k1} (n2 < kBigM, k1 < Cb, so n2 k1 < nfft: no reduction),
+  // then the Cb entries W_Cb^e = W_N^{e kBigM}
+  const uint32_t cb = gl.C;
+  std::vector<float2> twn((size_t)nfft + cb);
+  auto w_n = [nfft](uint64_t m) {
     const double a = -2.0 * M_PI * (double)m / (double)nfft;
-    twn[m] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
+    return make_float2((float)std::cos(a), (float)std::sin(a));
+  };
+  for (uint32_t k1 = 0; k1 < cb; ++k1)
+    for (uint32_t n2 = 0; n2 < kBigM; ++n2) twn[(size_t)k1 * kBigM + n2] = w_n((uint64_t)n2 * k1);
+  for (uint32_t e = 0; e < cb; ++e) twn[(size_t)nfft + e] = w_n((uint64_t)e * kBigM);
   cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
   if (e == cudaSuccess) e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&plan->d_tw_cross, twn.size() * sizeof(float2));

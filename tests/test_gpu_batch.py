@@ -80,3 +80,24 @@ def test_batch_autotune_keeps_results(spx, cuda):
     o2, c2 = b.run(xd)
     np.testing.assert_array_equal(c1.cpu().numpy(), c2.cpu().numpy())
     np.testing.assert_array_equal(spx.maxvalues_to_numpy(o1)["index"], spx.maxvalues_to_numpy(o2)["index"])
+
+
+@pytest.mark.parametrize("n_point,nfft", [(500000, 0), (4096, 1 << 20)])
+def test_batch_rejects_three_launch_sizes(spx, cuda, n_point, nfft):
+    """A beam whose transform is 2^19 or 2^20 points (the next 3-smooth size
+    of 500000 is 2^19, or an explicit nfft) is not a cluster of the batch
+    kernel: creation fails with SPX_ERR_UNSUPPORTED, nothing is launched, and
+    the context keeps working."""
+    from spectrum_gb300 import _capi
+    from spectrum_gb300.batch import Batch
+    n_points = [1000, n_point]
+    nffts = None if nfft == 0 else [0, nfft]
+    with pytest.raises(_capi.SpxError) as ei:
+        Batch(n_points, nffts=nffts, window=spx.WINDOW_HANN, k=4, sample_rate=1.0)
+    assert ei.value.status == _capi.SPX_ERR_UNSUPPORTED
+    assert "2^19 and 2^20" in str(ei.value)
+    lengths, flat = _uneven(6, 1000, 5000, seed=11)
+    b = Batch(lengths, window=spx.WINDOW_HANN, k=4, sample_rate=1.0)
+    import torch
+    out, counts = b.run(torch.from_numpy(flat).to(cuda))
+    assert int(counts.min()) >= 1
