@@ -153,6 +153,7 @@ fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ be
 // Top-K strict local maxima of every beam's spectrum (one CTA per beam),
 // the rules of topk_kernel (peak_kernels.cu) on packed, uneven spectra.
 constexpr uint32_t kBtThreads = 256;
+constexpr uint32_t kBtMaxC = 16;  // CTAs per beam in a batch (cluster size limit)
 
 SPX_DEV uint64_t bt_insert(uint64_t mine, uint64_t x, uint32_t lane) {
   const uint64_t up = __shfl_up_sync(0xffffffffu, mine, 1);
@@ -160,7 +161,58 @@ SPX_DEV uint64_t bt_insert(uint64_t mine, uint64_t x, uint32_t lane) {
   return (lane == 0 || up >= x) ? x : up;
 }
 
-__global__ void __launch_bounds__(kBtThreads)
+// The strict local maxima of bins [start, end) of one beam whose spectrum is
+// left in row layout (bin k in row k mod CC, column k div CC; rows M apart),
+// folded into the warp's sorted top-K list.  A lane owns column q: bins
+// q*CC + r (r < CC), one load per row, so a warp reads 32 consecutive
+// columns of each row (256 contiguous bytes) with CC loads in flight.  Each
+// |X| is computed once; the neighbours across a column edge come from the
+// next lane (or a load at the warp's edge).  The lists depend only on the set
+// of candidates, not on the order they are visited in.  The columns cover
+// bins start - 1 .. end.
+template <uint32_t CC>
+SPX_DEV uint64_t bt_scan(const float2* __restrict__ fs_row, uint32_t M, uint32_t start, uint32_t end,
+                         uint32_t K, uint32_t lane, uint32_t warp) {
+  auto bin = [&](uint32_t k) { return __ldg(fs_row + (size_t)(k % CC) * M + k / CC); };
+  uint64_t mine = 0;
+  const uint32_t q_lo = (start - 1) / CC, q_hi = end / CC;
+  for (uint32_t q0 = q_lo + warp * 32; q0 <= q_hi; q0 += kBtThreads) {
+    const uint32_t q = q0 + lane;
+    float2 z[CC];
+#pragma unroll
+    for (uint32_t r = 0; r < CC; ++r) {
+      const uint32_t k = q * CC + r;
+      z[r] = make_float2(0.f, 0.f);
+      if (q <= q_hi && k + 1 >= start && k <= end) z[r] = __ldg(fs_row + (size_t)r * M + q);
+    }
+    float m[CC];
+#pragma unroll
+    for (uint32_t r = 0; r < CC; ++r) m[r] = mag_rn(z[r]);
+    float left = __shfl_up_sync(0xffffffffu, m[CC - 1], 1);  // bin q*CC - 1
+    float right = __shfl_down_sync(0xffffffffu, m[0], 1);    // bin (q + 1)*CC
+    if (lane == 0 && q * CC >= start && q * CC < end) left = mag_rn(bin(q * CC - 1));
+    if (lane == 31 && q * CC + CC - 1 >= start && q * CC + CC - 1 < end) right = mag_rn(bin(q * CC + CC));
+#pragma unroll
+    for (uint32_t r = 0; r < CC; ++r) {
+      const uint32_t k = q * CC + r;
+      const float c = m[r];
+      const float lft = r == 0 ? left : m[r == 0 ? 0 : r - 1];
+      const float rgt = r + 1 == CC ? right : m[r + 1 < CC ? r + 1 : r];
+      const bool cand = q <= q_hi && k >= start && k < end && c > lft && c > rgt;
+      const uint64_t key = ((uint64_t)__float_as_uint(c) << 32) | (uint32_t)(~k);
+      const uint64_t kth = __shfl_sync(0xffffffffu, mine, K - 1);
+      uint32_t want = __ballot_sync(0xffffffffu, cand && key > kth);
+      while (want) {
+        const int src = __ffs(want) - 1;
+        want &= want - 1;
+        mine = bt_insert(mine, __shfl_sync(0xffffffffu, key, src), lane);
+      }
+    }
+  }
+  return mine;
+}
+
+__global__ void __launch_bounds__(kBtThreads, 4)
 topk_batch_kernel(const float2* __restrict__ xch, const BatchBeam* __restrict__ beams,
                   const BatchGeom* __restrict__ geoms, const uint32_t* __restrict__ beam_list, uint32_t K,
                   uint32_t start0, uint32_t end0, float fs, uint32_t refine, MaxValueDev* __restrict__ out,
@@ -182,22 +234,16 @@ topk_batch_kernel(const float2* __restrict__ xch, const BatchBeam* __restrict__ 
   };
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t mine = 0;
-  for (uint32_t base = start + warp * 32; base < end; base += kBtThreads) {
-    const uint32_t k = base + lane;
-    uint64_t key = 0;
-    bool cand = false;
-    if (k < end) {
-      const float c = mag_rn(bin(k));
-      cand = (c > mag_rn(bin(k - 1))) && (c > mag_rn(bin(k + 1)));
-      key = ((uint64_t)__float_as_uint(c) << 32) | (uint32_t)(~k);
-    }
-    const uint64_t kth = __shfl_sync(0xffffffffu, mine, K - 1);
-    uint32_t want = __ballot_sync(0xffffffffu, cand && key > kth);
-    while (want) {
-      const int src = __ffs(want) - 1;
-      want &= want - 1;
-      mine = bt_insert(mine, __shfl_sync(0xffffffffu, key, src), lane);
-    }
+  switch (C) {  // the same for the whole CTA
+    case 1: mine = bt_scan<1>(fs_row, M, start, end, K, lane, warp); break;
+    case 2: mine = bt_scan<2>(fs_row, M, start, end, K, lane, warp); break;
+    case 3: mine = bt_scan<3>(fs_row, M, start, end, K, lane, warp); break;
+    case 4: mine = bt_scan<4>(fs_row, M, start, end, K, lane, warp); break;
+    case 6: mine = bt_scan<6>(fs_row, M, start, end, K, lane, warp); break;
+    case 8: mine = bt_scan<8>(fs_row, M, start, end, K, lane, warp); break;
+    case 9: mine = bt_scan<9>(fs_row, M, start, end, K, lane, warp); break;
+    case 12: mine = bt_scan<12>(fs_row, M, start, end, K, lane, warp); break;
+    default: mine = bt_scan<16>(fs_row, M, start, end, K, lane, warp); break;
   }
   lists[warp][lane] = mine;
   __syncthreads();
@@ -323,6 +369,7 @@ spx_status build_launches(spx_ctx* ctx, spx_batch* b) {
       const FftPlan* plan = nullptr;
       spx_status st = get_plan(ctx, n, &plan);
       if (st != SPX_OK) return st;
+      if (plan->big || plan->g.C > kBtMaxC) return fail(ctx, SPX_ERR_UNSUPPORTED, "batch: nfft " + std::to_string(n));
       geom_of[n] = (uint32_t)geoms.size();
       geoms.push_back(BatchGeom{plan->g, plan->d_tw_local, plan->d_tw_cross});
     }
@@ -355,8 +402,12 @@ spx_status build_launches(spx_ctx* ctx, spx_batch* b) {
     ls->ept = b->ept;
     ls->smem = (size_t)mpad * sizeof(float2);
     ls->n_beams = (uint32_t)ids.size();
+    // the top-K kernel visits the largest spectra first (outputs are indexed by beam)
+    std::vector<uint32_t> by_size(ids);
+    std::stable_sort(by_size.begin(), by_size.end(),
+                     [&](uint32_t x, uint32_t y) { return b->nfft[x] > b->nfft[y]; });
     spx_status s2 = upload(ctx, b, ctas, &ls->d_ctas);
-    if (s2 == SPX_OK) s2 = upload(ctx, b, ids, &ls->d_beam_list);
+    if (s2 == SPX_OK) s2 = upload(ctx, b, by_size, &ls->d_beam_list);
     return s2;
   };
   std::vector<uint32_t> all(b->beams);
