@@ -134,17 +134,17 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
   }
   const float bw = __fdiv_rn(a.fs, (float)g.nfft);
   if (a.mode == SPX_PEAK_TOPK) {
-    // one descending list per warp (lane l holds entry l), merged by warp 0
+    // one descending list per warp (lane l holds entry l), merged by warp 0;
+    // |X| of bins start .. end computed once, neighbours from the next lanes
     uint64_t mine = 0;
     for (uint32_t base = a.start + warp * 32; base < a.end; base += T) {
       const uint32_t k = base + lane;
-      uint64_t key = 0;
-      bool cand = false;
-      if (k < a.end) {
-        const float c = mag_rn(s[sw(k)]);
-        cand = (c > mag_rn(s[sw(k - 1)])) && (c > mag_rn(s[sw(k + 1)])) && (c > thr);
-        key = ((uint64_t)__float_as_uint(c) << 32) | (uint32_t)(~k);
-      }
+      const float c = k <= a.end ? mag_rn(s[sw(k)]) : 0.f;
+      float lft = __shfl_up_sync(0xffffffffu, c, 1), rgt = __shfl_down_sync(0xffffffffu, c, 1);
+      if (lane == 0 && k < a.end) lft = mag_rn(s[sw(k - 1)]);
+      if (lane == 31 && k < a.end) rgt = mag_rn(s[sw(k + 1)]);
+      const bool cand = k < a.end && c > lft && c > rgt && c > thr;
+      const uint64_t key = ((uint64_t)__float_as_uint(c) << 32) | (uint32_t)(~k);
       const uint64_t kth = __shfl_sync(0xffffffffu, mine, a.K - 1);
       uint32_t want = __ballot_sync(0xffffffffu, cand && key > kth);
       while (want) {
@@ -178,16 +178,16 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
     }
     return;
   }
-  // ALL: ordered compaction over [start, end) in rounds of T consecutive bins.
+  // ALL: ordered compaction over [start, end) in rounds of T consecutive bins
+  // (|X| once per bin, neighbours from the next lanes).
   uint32_t total = 0;
   for (uint32_t base = a.start; base < a.end; base += T) {
     const uint32_t k = base + tid;
-    bool f = false;
-    float c = 0.f;
-    if (k < a.end) {
-      c = mag_rn(s[sw(k)]);
-      f = (c > mag_rn(s[sw(k - 1)])) && (c > mag_rn(s[sw(k + 1)])) && (c > thr);
-    }
+    const float c = k <= a.end ? mag_rn(s[sw(k)]) : 0.f;
+    float lft = __shfl_up_sync(0xffffffffu, c, 1), rgt = __shfl_down_sync(0xffffffffu, c, 1);
+    if (lane == 0 && k < a.end) lft = mag_rn(s[sw(k - 1)]);
+    if (lane == 31 && k < a.end) rgt = mag_rn(s[sw(k + 1)]);
+    const bool f = k < a.end && c > lft && c > rgt && c > thr;
     const uint32_t b = __ballot_sync(0xffffffffu, f);
     if (lane == 0) s_red[warp] = __popc(b);
     __syncthreads();
@@ -199,9 +199,7 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
     }
     if (f) {
       const uint32_t rank = before + __popc(b & ((1u << lane) - 1u));
-      if (rank < a.cap)
-        a.out[(size_t)beam * a.cap + rank] =
-            fused_max(k, s[sw(k)], mag_rn(s[sw(k - 1)]), c, mag_rn(s[sw(k + 1)]), bw, a.refine);
+      if (rank < a.cap) a.out[(size_t)beam * a.cap + rank] = fused_max(k, s[sw(k)], lft, c, rgt, bw, a.refine);
     }
     total += all;
     __syncthreads();
