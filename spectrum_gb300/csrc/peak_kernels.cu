@@ -495,6 +495,7 @@ uint64_t all_maxima_tiles(uint32_t beams, uint32_t start, uint32_t end) {
 // ---------------------------------------------------------------------------
 constexpr uint32_t kTkThreads = 256;
 constexpr uint32_t kTkWarps = kTkThreads / 32;
+constexpr uint32_t kTkRun = 8;  // runs of 32 bins per warp step
 
 // Key orders by |X| descending, then bin ascending; 0 = empty slot.
 SPX_DEV uint64_t topk_key(float mag, uint32_t bin) {
@@ -523,24 +524,50 @@ topk_kernel(const float* __restrict__ mag, const float2* __restrict__ fft, uint3
   const size_t bb = (size_t)beam * nfft;
   const float thr = thrs ? thrs[beam] : -INFINITY;
   uint64_t mine = 0;  // this lane's list entry
-  for (uint32_t base = start + warp * 32; base < end; base += kTkThreads) {
-    const uint32_t bin = base + lane;
-    uint64_t key = 0;
-    bool cand = false;
-    if (bin < end) {
-      const float c = mag_at(mag, fft, bb + bin);
-      const float l = mag_at(mag, fft, bb + bin - 1);
-      const float r = mag_at(mag, fft, bb + bin + 1);
-      cand = (c > l) && (c > r) && (c > thr);
-      key = topk_key(c, bin);
+  // A warp step covers kTkRun runs of 32 consecutive bins (bin base + 32j +
+  // lane): kTkRun loads in flight per lane, 128- or 256-byte warp reads, each
+  // |X| computed once and the neighbours taken from the adjacent lanes (or
+  // runs; two loads at the step's edges).  Bins start - 1 .. end are read.
+  for (uint32_t base = start + warp * 32 * kTkRun; base < end; base += kTkThreads * kTkRun) {
+    float m[kTkRun];
+    if (mag) {
+#pragma unroll
+      for (uint32_t j = 0; j < kTkRun; ++j) {
+        const uint32_t b = base + 32 * j + lane;
+        m[j] = b <= end ? __ldg(mag + bb + b) : 0.f;
+      }
+    } else {
+      float2 z[kTkRun];
+#pragma unroll
+      for (uint32_t j = 0; j < kTkRun; ++j) {
+        const uint32_t b = base + 32 * j + lane;
+        z[j] = b <= end ? __ldg(fft + bb + b) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < kTkRun; ++j) m[j] = mag_rn(z[j]);
     }
-    const uint64_t kth = __shfl_sync(0xffffffffu, mine, K - 1);
-    uint32_t want = __ballot_sync(0xffffffffu, cand && key > kth);
-    while (want) {
-      const int src = __ffs(want) - 1;
-      want &= want - 1;
-      const uint64_t x = __shfl_sync(0xffffffffu, key, src);
-      mine = list_insert(mine, x, lane);
+    float edge = 0.f;  // lane 0: bin base - 1; lane 31: bin base + 32 kTkRun
+    if (lane == 0) edge = mag_at(mag, fft, bb + base - 1);
+    if (lane == 31 && base + 32 * kTkRun <= end) edge = mag_at(mag, fft, bb + base + 32 * kTkRun);
+#pragma unroll
+    for (uint32_t j = 0; j < kTkRun; ++j) {
+      const uint32_t b = base + 32 * j + lane;
+      const float prev_last = __shfl_sync(0xffffffffu, m[j == 0 ? 0 : j - 1], 31);
+      const float next_first = __shfl_sync(0xffffffffu, m[j + 1 < kTkRun ? j + 1 : j], 0);
+      float l = __shfl_up_sync(0xffffffffu, m[j], 1), r = __shfl_down_sync(0xffffffffu, m[j], 1);
+      if (lane == 0) l = j == 0 ? edge : prev_last;
+      if (lane == 31) r = j + 1 == kTkRun ? edge : next_first;
+      const float c = m[j];
+      const bool cand = b < end && c > l && c > r && c > thr;
+      const uint64_t key = topk_key(c, b);
+      const uint64_t kth = __shfl_sync(0xffffffffu, mine, K - 1);
+      uint32_t want = __ballot_sync(0xffffffffu, cand && key > kth);
+      while (want) {
+        const int src = __ffs(want) - 1;
+        want &= want - 1;
+        const uint64_t x = __shfl_sync(0xffffffffu, key, src);
+        mine = list_insert(mine, x, lane);
+      }
     }
   }
   lists[warp][lane] = mine;
