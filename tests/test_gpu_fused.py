@@ -158,15 +158,16 @@ def test_fft_peaks_host_matches_device_path(spx, cuda, nfft, n_point, beams, mod
     else:
         xh = xh.numpy()
     oh, ch = spx.fft_peaks_host(xh, nfft, spx.WINDOW_HANN, m, **kw)
-    if pinned:  # page-locked outputs as well: the kernel writes the peaks in place
-        oh2 = torch.zeros(oh.shape, dtype=oh.dtype).pin_memory()
-        ch2 = torch.zeros(ch.shape, dtype=ch.dtype).pin_memory()
-        spx.fft_peaks_host(xh, nfft, spx.WINDOW_HANN, m, out=oh2, counts=ch2, **kw)
-        np.testing.assert_array_equal(ch2.numpy(), ch.numpy())
-        g1, g2 = spx.maxvalues_to_numpy(oh), spx.maxvalues_to_numpy(oh2)
-        for b in range(beams):
-            n = int(ch[b]) if mode != "one" else g1.shape[1]
-            np.testing.assert_array_equal(g2[b, :n], g1[b, :n])
+    # page-locked outputs as well: the kernel writes the peaks in place (also
+    # behind chunked uploads of pageable input)
+    oh2 = torch.zeros(oh.shape, dtype=oh.dtype).pin_memory()
+    ch2 = torch.zeros(ch.shape, dtype=ch.dtype).pin_memory()
+    spx.fft_peaks_host(xh, nfft, spx.WINDOW_HANN, m, out=oh2, counts=ch2, **kw)
+    np.testing.assert_array_equal(ch2.numpy(), ch.numpy())
+    g1, g2 = spx.maxvalues_to_numpy(oh), spx.maxvalues_to_numpy(oh2)
+    for b in range(beams):
+        n = int(ch[b]) if mode != "one" else g1.shape[1]
+        np.testing.assert_array_equal(g2[b, :n], g1[b, :n])
     gd, gh = spx.maxvalues_to_numpy(od), spx.maxvalues_to_numpy(oh)
     if mode == "one":
         np.testing.assert_array_equal(gh, gd)
