@@ -296,7 +296,10 @@ spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
  * No reference counterpart (DspSpectrum transforms one nFFT per call).  A
  * batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->
  * spx_next_smooth23(n_point)), the window and TOPK peak parameters
- * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Inputs are
+ * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Every
+ * nfft must run as one CTA or one cluster of at most 16 CTAs: 2^19 and
+ * 2^20 (three-launch transforms) return SPX_ERR_UNSUPPORTED; run them
+ * through spx_fft_peaks.  Inputs are
  * packed: beam i's samples start at sum_{j<i} n_point[j] (complex64); outputs
  * are [B x K] MaxValue and [B] counts.  Device scratch is owned by the batch.
  *  spx_batch_run           all beams in ONE FFT launch + one top-K launch
