@@ -152,6 +152,28 @@ def test_topk(spx, cuda, nfft, k, kind):
         assert_maxvalues_equal(got[b], ref[b], n=int(rcounts[b]))
 
 
+@pytest.mark.parametrize("nfft,start,end,k", [
+    (4096, 37, 1000, 5),        # unaligned window over several warp steps
+    (4096, 1, 20, 8),           # window narrower than one run of 32 bins
+    (8192, 3000, 8191, 16),     # window ending at the last bin
+    (65536, 5, 40000, 32),      # many 2048-bin steps, K = 32
+])
+@pytest.mark.parametrize("with_mag", [False, True])
+def test_topk_windows_and_magnitude_input(spx, cuda, nfft, start, end, k, with_mag):
+    """spx_topk over search windows of any start and length, including one
+    ending at the last bin, and over a caller's magnitude array (independent
+    of the spectrum, so the kernel must take |X| from it): the oracle's lists."""
+    z = _noise_spectrum(3, nfft, 17, tones=6)
+    mag = np.random.default_rng(5).random((3, nfft), dtype=np.float32) if with_mag else None
+    out, counts = spx.topk(_dev(z, cuda), k, None if mag is None else _dev(mag, cuda), 1000.0,
+                           search_start=start, search_end=end)
+    ref, rcounts = orc.topk(mag, z, nfft, 1000.0, k, start, end)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rcounts)
+    got = spx.maxvalues_to_numpy(out)
+    for b in range(3):
+        assert_maxvalues_equal(got[b], ref[b], n=int(rcounts[b]))
+
+
 def test_topk_with_threshold(spx, cuda):
     z = _noise_spectrum(3, 8192, 5, tones=4)
     out, counts = spx.topk(_dev(z, cuda), 16, None, 1.0, thresh_sigma=6.0)
