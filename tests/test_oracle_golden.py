@@ -94,6 +94,21 @@ def test_known_answer_100hz():
     assert abs(got[0]["refined_frequency"] - 100.0) < 5.0
 
 
+def test_known_answer_16_beams():
+    """tests/test_spectrum_maxima_rocm.hpp:196-233: 16 beams of sin(2 pi f t / fs) with
+    f = 100 + 10 b Hz, fs 10 kHz, 1000 points, ONE_PEAK -> |refined f - f| < 10 Hz."""
+    fs, n = 10000.0, 1000
+    t = np.arange(n, dtype=np.float32)
+    x = np.zeros((16, n), np.complex64)
+    for b in range(16):
+        f = np.float32(100.0 + 10.0 * b)
+        x[b].real = np.sin(np.float32(2.0 * np.pi) * f * t / np.float32(fs))
+    got = orc.one_two_peaks(orc.fft_fp32(x, 1024), 1024, 0, fs, False)
+    assert got.shape == (16, 4)
+    for b in range(16):
+        assert abs(float(got[b, 0]["refined_frequency"]) - (100.0 + 10.0 * b)) < 10.0
+
+
 def test_known_answer_spikes():
     """tests/test_spectrum_maxima_rocm.hpp:179-206: spikes at 50/120/200 on a 0.1 floor."""
     z = np.full((1, 1024), 0.1, np.complex64)
