@@ -86,3 +86,20 @@ def test_null_context_is_invalid_argument(lib):
     assert lib.spx_fft(None, None, 1, 1, 1, 0, 0, 1.0, None) == 1
     assert lib.spx_destroy(None) == 0
     assert lib.spx_last_error(None) == b""
+
+
+def test_every_entry_point_rejects_null_handles(lib):
+    """Every call whose first argument is a context, batch or MLP handle returns
+    SPX_ERR_INVALID_ARG for null handles and zero sizes, before it touches a
+    device; the destroy calls accept null, like free()."""
+    from spectrum_gb300 import _capi
+    destroy = {"spx_destroy", "spx_batch_destroy", "spx_mlp_destroy"}
+    checked = 0
+    for name, (res, args) in _capi.PROTOTYPES.items():
+        if res is not C.c_int or not args or args[0] is not C.c_void_p:
+            continue
+        vals = [0.0 if a is C.c_float else 0 if a in (C.c_uint32, C.c_int, C.c_uint64) else None
+                for a in args]
+        assert getattr(lib, name)(*vals) == (0 if name in destroy else 1), name
+        checked += 1
+    assert checked >= 30
