@@ -103,3 +103,26 @@ def test_every_entry_point_rejects_null_handles(lib):
         assert getattr(lib, name)(*vals) == (0 if name in destroy else 1), name
         checked += 1
     assert checked >= 30
+
+
+@pytest.mark.parametrize("call", ["fft", "ifft", "fft_r2c", "topk", "all_maxima", "fft_peaks",
+                                  "host_dtype", "host_strided"])
+def test_python_wrappers_reject_bad_tensors_before_any_device_work(lib, call):
+    """The Python mirror checks device, dtype and layout first, like the
+    reference's std::invalid_argument checks, and raises ValueError."""
+    import torch
+
+    import spectrum_gb300 as spx
+    x = torch.zeros((2, 64), dtype=torch.complex64)
+    calls = {
+        "fft": lambda: spx.fft(x, 64),
+        "ifft": lambda: spx.ifft(x),
+        "fft_r2c": lambda: spx.fft_r2c(torch.zeros((2, 64)), 64),
+        "topk": lambda: spx.topk(x, 5),
+        "all_maxima": lambda: spx.all_maxima(x),
+        "fft_peaks": lambda: spx.fft_peaks(x, 64),
+        "host_dtype": lambda: spx.fft_peaks_host(torch.zeros((2, 64)), 64),
+        "host_strided": lambda: spx.fft_peaks_host(x.t(), 64),
+    }
+    with pytest.raises(ValueError):
+        calls[call]()
