@@ -14,7 +14,10 @@ of the maxima and counts inside the timed region.
 
 --impl reference times the reference's CPU path on the host cores instead:
 pocketfft FP32 (scipy.fft, the library the reference vendors for its CPU FFT)
-+ the CPU restatement of |X| and the peak search, on a bounded sample.
++ the CPU restatement of |X| and the peak search, on all 256 beams of the
+same workload per step.  That arm never imports the spectrum_gb300 package
+(whose __init__ loads the native library): it loads the seeded generator
+spectrum_gb300/synth.py by file path.
 """
 from __future__ import annotations
 
@@ -36,9 +39,13 @@ BEAMS, N_POINT, NFFT = 256, 65536, 131072
 FS = 1.0
 SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
-# DRAM bytes (read + write) of one step on this workload (fft_group_kernel +
-# maxima_cluster_kernel), from an ncu capture (profiles/fft_group_kernel_plain_large.md).
+# DRAM bytes (read + write) of one step on this workload, the sum of
+# dram__bytes_read.sum + dram__bytes_write.sum of fft_group_kernel<16384> and
+# maxima_cluster_kernel from one ncu capture; NCU_TRAFFIC_KERNELS names the
+# kernels it covers and the commit it was taken at, so a change of either
+# shows that the figure must be captured again.
 NCU_TRAFFIC_BYTES = 359_430_912
+NCU_TRAFFIC_KERNELS = {"kernels": ["fft_group_kernel<16384>", "maxima_cluster_kernel"], "commit": "ccafa54"}
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
@@ -123,14 +130,14 @@ def job_throughput(world_size: int, ms: float) -> float:
 # ---------------------------------------------------------------------------
 # CPU path (reference arm and cpu_baseline)
 # ---------------------------------------------------------------------------
-def cpu_path_sample(x: np.ndarray, workers: int):
-    """pocketfft FP32 FFT over the beams (scipy.fft, `workers` threads) + |X| +
-    thresholded all-maxima search; returns the number of maxima found."""
+def _cpu_beams(x: np.ndarray) -> int:
+    """One host thread's share: pocketfft FP32 FFT (scipy.fft, one thread) +
+    |X| + thresholded all-maxima search of its beams; the number of maxima."""
     import scipy.fft as sf
 
     from oracle import spectrum_oracle as orc
     xw = orc.windowed(x, orc.WINDOW_HANN)
-    spec = sf.fft(xw, n=NFFT, axis=-1, workers=workers)
+    spec = sf.fft(xw, n=NFFT, axis=-1, workers=1)
     assert spec.dtype == np.complex64
     mag = orc.mag_rn(spec)
     start, end, cap = orc.all_maxima_capacity(NFFT, 0, 0, 1000)
@@ -141,8 +148,37 @@ def cpu_path_sample(x: np.ndarray, workers: int):
     return total
 
 
+_POOL = None
+
+
+def cpu_path_sample(x: np.ndarray, workers: int):
+    """The CPU path over the beams, spread over `workers` host threads by beam
+    ranges (numpy and pocketfft release the GIL); returns the number of
+    maxima found."""
+    from concurrent.futures import ThreadPoolExecutor
+    global _POOL
+    if _POOL is None or _POOL._max_workers != workers:
+        _POOL = ThreadPoolExecutor(max_workers=workers)
+    parts = [p for p in np.array_split(np.arange(x.shape[0]), workers) if len(p)]
+    return sum(_POOL.map(lambda p: _cpu_beams(x[p[0]:p[-1] + 1]), parts))
+
+
+def _synth():
+    """spectrum_gb300/synth.py loaded by file path: the seeded generator
+    without the package __init__ (which loads the native library)."""
+    import importlib.util
+    mod = sys.modules.get("spectrum_gb300_synth")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("spectrum_gb300_synth",
+                                                      os.path.join(ROOT, "spectrum_gb300", "synth.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["spectrum_gb300_synth"] = mod
+        spec.loader.exec_module(mod)
+    return mod
+
+
 def cpu_measure(sample_beams: int, reps_budget_s: float = 15.0):
-    from spectrum_gb300 import synth
+    synth = _synth()
     bs = synth.workload_large(seed=1, beams=sample_beams)
     x = synth.synth_numpy(bs)
     cores = os.cpu_count() or 1
@@ -156,16 +192,17 @@ def cpu_measure(sample_beams: int, reps_budget_s: float = 15.0):
             break
     dt = (time.perf_counter() - t0) / reps
     msps = sample_beams * N_POINT / dt / 1e6
-    return msps, cores, f"{sample_beams} beams x {N_POINT} of the same workload, {reps} repetitions"
+    return msps, cores, (f"{sample_beams} beams x {N_POINT} of the same workload, {reps} repetitions, beam ranges "
+                         f"spread over {cores} host threads")
 
 
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
         return
-    beams = args.cpu_sample_beams or 16
-    # each step is one bounded sample; warmup + steps sized to stay within minutes
-    from spectrum_gb300 import synth
+    # each step is the whole workload (256 beams, ~0.25 s of CPU work on 16 cores)
+    beams = args.cpu_sample_beams or BEAMS
+    synth = _synth()
     bs = synth.workload_large(seed=1, beams=beams)
     x = synth.synth_numpy(bs)
     cores = os.cpu_count() or 1
@@ -183,10 +220,12 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(step * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_beams": beams, "cpu_threads": cores},
+        "config": {"workload": WORKLOAD, "beams": beams, "n_point": N_POINT, "nfft": NFFT, "window": "hann",
+                   "thresh_sigma": SIGMA, "refine": "parabolic", "cpu_threads": cores},
         "cpu_baseline": {"value": round(value, 3), "unit": "Msamples/s", "cores": cores, "kind": "port",
                          "sample": f"{beams} beams x {N_POINT} per step (pocketfft FP32 via scipy.fft + "
-                                   f"CPU restatement of |X| and the thresholded all-maxima search)"},
+                                   f"CPU restatement of |X| and the thresholded all-maxima search, beam "
+                                   f"ranges spread over {cores} host threads)"},
         "e2e": {"value": round(value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -346,7 +385,7 @@ def run_gpu(args):
     r = line["roofline"]
     r["frac"] = round(r["achieved"] / r["peak"], 4)
     if args.cpu_sample_beams >= 0:
-        v, cores, sample = cpu_measure(args.cpu_sample_beams or 8)
+        v, cores, sample = cpu_measure(args.cpu_sample_beams or BEAMS, reps_budget_s=10.0)
         line["cpu_baseline"] = {"value": round(v, 3), "unit": "Msamples/s", "cores": cores, "kind": "port",
                                 "sample": sample}
     print(json.dumps(line), flush=True)
@@ -402,7 +441,7 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
                      "achieved": round(algo / (f * 1e-3) / 1e9, 1),
                      "unit": "GB/s", "traffic": NCU_TRAFFIC_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of each "
-                                       "kernel (profiles/fft_group_kernel_plain_large.md)",
+                                       "kernel of the step", "traffic_captured": NCU_TRAFFIC_KERNELS,
                      "algorithmic_bytes_per_launch": algo,
                      "maxima_per_launch": n_max},
         "launches_per_step": 2,

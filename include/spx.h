@@ -143,6 +143,11 @@ spx_status spx_synchronize(spx_ctx* ctx);
 const char* spx_last_error(const spx_ctx* ctx);
 const char* spx_status_string(spx_status status);
 int spx_abi_version(void);
+/* Bytes of grow-on-demand device scratch ctx holds now (look-back words,
+ * thresholds, intermediate spectra, exchange slots), for memory accounting;
+ * 0 for a context no call has needed scratch on yet.  No reference
+ * counterpart (the reference's BufferSet does not report its size). */
+uint64_t spx_scratch_bytes(const spx_ctx* ctx);
 
 /* Self-test of the bounded device-side waits (no reference counterpart).
  * Every spin-wait in this library's kernels (the look-back of the all-maxima
@@ -250,7 +255,9 @@ spx_status spx_topk(spx_ctx* ctx, const float* d_mag, const void* d_fft,
  *    by every GPU that loads the library until exit and shared by all calls:
  *    calls whose kernels overlap on the GPU race, so order them on one stream;
  *  - the first call on a device looks the array's address up (once, with that
- *    device current); make it before any stream capture.
+ *    device current) and, under CUDA's lazy module loading, loads the modules
+ *    of the array and of the search kernel, which can allocate device memory
+ *    once: make it during set-up, before any stream capture.
  * ctx is only used for its stream and error reporting (spx_create allocates
  * its small state once, before the no-allocation phase). */
 spx_status spx_all_maxima_noalloc(spx_ctx* ctx, const float* d_mag, const void* d_fft,

@@ -73,6 +73,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_last_error": (C.c_char_p, [_vp]),
     "spx_status_string": (C.c_char_p, [_i]),
     "spx_abi_version": (_i, []),
+    "spx_scratch_bytes": (_u64, [_vp]),
     "spx_selftest_wait_timeout": (_i, [_vp]),
     "spx_selftest_group_wait_timeout": (_i, [_vp]),
     "spx_next_pow2": (_u32, [_u32]),

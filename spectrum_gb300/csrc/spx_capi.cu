@@ -85,6 +85,13 @@ extern "C" {
 
 int spx_abi_version(void) { return SPX_ABI_VERSION; }
 
+uint64_t spx_scratch_bytes(const spx_ctx* ctx) {
+  if (!ctx) return 0;
+  uint64_t n = 0;
+  for (size_t b : ctx->scratch_bytes) n += b;
+  return n;
+}
+
 const char* spx_status_string(spx_status s) {
   switch (s) {
     case SPX_OK: return "SPX_OK";

@@ -86,6 +86,7 @@ def test_null_context_is_invalid_argument(lib):
     assert lib.spx_fft(None, None, 1, 1, 1, 0, 0, 1.0, None) == 1
     assert lib.spx_destroy(None) == 0
     assert lib.spx_last_error(None) == b""
+    assert lib.spx_scratch_bytes(None) == 0
 
 
 def test_every_entry_point_rejects_null_handles(lib):

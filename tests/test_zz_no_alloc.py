@@ -44,6 +44,10 @@ def _run(spx, lib_fn, ctx, z_dev, mag_dev, beams, nfft, params, cap, bufs=None):
 
 
 def test_noalloc_matches_all_maxima_two_calls(spx, cuda):
+    """The expected lists come from spx_all_maxima on the default context; the
+    calls under test run on a context of their own, created here, whose
+    grow-on-demand scratch no call has touched: a no-allocation call routed
+    through that scratch would make it non-zero."""
     import torch
     ctx = spx.default_context()
     cases = [
@@ -63,14 +67,17 @@ def test_noalloc_matches_all_maxima_two_calls(spx, cuda):
 
     # output buffers first, so that nothing but the call under test could allocate below
     bufs = [_outputs(d[0], d[2], d[5]) for d in data]
-    # warm-up call: resolves the fixed scratch array's address on this device
+    fresh = spx.Context(cuda.index or 0)
+    assert spx.lib.spx_scratch_bytes(fresh.h) == 0
+    # set-up call: resolves the fixed array's address on this device and loads
+    # the kernel's module (the first call on a device may allocate doing so)
     z, mag, beams, nfft, p, cap, _ = data[0]
-    _run(spx, spx.lib.spx_all_maxima_noalloc, ctx, z, mag, beams, nfft, p, cap, bufs[0])
+    _run(spx, spx.lib.spx_all_maxima_noalloc, fresh, z, mag, beams, nfft, p, cap, bufs[0])
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
 
     for (z, mag, beams, nfft, p, cap, (ref_out, ref_counts)), buf in zip(data, bufs):
-        out, counts = _run(spx, spx.lib.spx_all_maxima_noalloc, ctx, z, mag, beams, nfft, p, cap, buf)
+        out, counts = _run(spx, spx.lib.spx_all_maxima_noalloc, fresh, z, mag, beams, nfft, p, cap, buf)
         torch.cuda.synchronize()
         rc = ref_counts.cpu().numpy()
         np.testing.assert_array_equal(counts.cpu().numpy(), rc)
@@ -84,8 +91,11 @@ def test_noalloc_matches_all_maxima_two_calls(spx, cuda):
             assert n > 0
 
     torch.cuda.synchronize()
+    assert spx.lib.spx_scratch_bytes(fresh.h) == 0, "the no-allocation entry point grew the context's scratch"
     assert torch.cuda.mem_get_info()[0] == free_before, "the no-allocation entry point allocated device memory"
-    ctx.synchronize()  # no bounded device wait expired
+    fresh.synchronize()  # no bounded device wait expired
+    fresh.close()
+    ctx.synchronize()
 
 
 def test_noalloc_rejects_what_it_cannot_serve(spx, cuda):
