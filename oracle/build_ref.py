@@ -15,7 +15,9 @@ the repository:
 
 Plain g++ on those few files, no build system of the reference.  FP
 contraction is disabled so ``x*x + y*y`` rounds each operation, as numpy does.
-Set SPX_REFERENCE_ROOT to point at another copy of the reference.
+The reference's location comes from the caller (``build(root)``,
+``reference_present(root)``) or from the SPX_REFERENCE_ROOT environment
+variable; this file assumes no path of its own.
 """
 from __future__ import annotations
 
@@ -26,14 +28,19 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF = Path(os.environ.get("SPX_REFERENCE_ROOT", "/root/reference"))
 
 CXX = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math"]
 
 
-def reference_present() -> bool:
-    return (REF / "include" / "spectrum" / "utils" / "cpu_fft.hpp").exists() and \
-        (REF / "include" / "spectrum" / "kernels" / "all_maxima_kernel_sources_rocm.hpp").exists()
+def _root(root) -> Path | None:
+    r = root or os.environ.get("SPX_REFERENCE_ROOT")
+    return Path(r) if r else None
+
+
+def reference_present(root=None) -> bool:
+    ref = _root(root)
+    return ref is not None and (ref / "include" / "spectrum" / "utils" / "cpu_fft.hpp").exists() and \
+        (ref / "include" / "spectrum" / "kernels" / "all_maxima_kernel_sources_rocm.hpp").exists()
 
 
 def _run(cmd):
@@ -53,12 +60,13 @@ def _sanitize(text: str) -> str:
     return text
 
 
-def build(force: bool = False) -> dict:
-    if not reference_present():
-        raise FileNotFoundError(f"reference sources not found under {REF}")
+def build(root=None, force: bool = False) -> dict:
+    ref = _root(root)
+    if not reference_present(ref):
+        raise FileNotFoundError(f"reference sources not found under {ref} (give root or SPX_REFERENCE_ROOT)")
     OUT.mkdir(exist_ok=True)
-    inc = REF / "include"
-    pocket = REF / "third_party" / "pocketfft"
+    inc = ref / "include"
+    pocket = ref / "third_party" / "pocketfft"
     libs = {"cpufft": OUT / "libref_cpufft.so", "kernels": OUT / "libref_kernels.so"}
 
     def stale(lib: Path, *srcs: Path) -> bool:
@@ -81,4 +89,5 @@ def build(force: bool = False) -> dict:
 
 
 if __name__ == "__main__":
-    print(build(force=True))
+    import sys
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None, force=True))

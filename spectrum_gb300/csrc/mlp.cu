@@ -92,24 +92,40 @@ __global__ void mlp_bwd_data_kernel(const float* __restrict__ dZ, const __nv_bfl
   dX[idx] = acc * gelu_grad(Zprev[idx]);
 }
 
-// dW[o][i] += sum_b dZ[b][o] X[b][i];  db[o] += sum_b dZ[b][o].
-// blockIdx.y takes a chunk of kBwdChunk rows; partial sums meet in atomics.
+// Partial weight gradients of one chunk of kBwdChunk rows (blockIdx.y):
+// part[chunk][o*in + i] = sum_b dZ[b][o] X[b][i] and part[chunk][out*in + o]
+// = sum_b dZ[b][o] over the chunk's rows b, in row order.  mlp_sum_chunks
+// then adds the chunks in chunk order: the gradient is the same bits on every
+// run (no atomics), so training is reproducible.
 constexpr uint32_t kBwdChunk = 512;
+constexpr uint32_t kMaxLayerParams = kH * (kH + 1);  // largest out * (in + 1)
 __global__ void mlp_bwd_weight_kernel(const float* __restrict__ dZ, const float* __restrict__ X,
-                                      uint32_t B, int in, int out, float* __restrict__ dW,
-                                      float* __restrict__ db) {
+                                      uint32_t B, int in, int out, float* __restrict__ part) {
   const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (uint32_t)(out * (in + 1))) return;
+  const uint32_t n = (uint32_t)(out * (in + 1));
+  if (idx >= n) return;
   const uint32_t o = idx / (in + 1), i = idx % (in + 1);
   const uint32_t b0 = blockIdx.y * kBwdChunk, b1 = min(B, b0 + kBwdChunk);
   float acc = 0.f;
+  float* dst = part + (size_t)blockIdx.y * n;
   if (i < (uint32_t)in) {
     for (uint32_t b = b0; b < b1; ++b) acc = fmaf(dZ[(size_t)b * out + o], X[(size_t)b * in + i], acc);
-    atomicAdd(&dW[(size_t)o * in + i], acc);
+    dst[o * in + i] = acc;
   } else {
     for (uint32_t b = b0; b < b1; ++b) acc += dZ[(size_t)b * out + o];
-    atomicAdd(&db[o], acc);
+    dst[out * in + o] = acc;
   }
+}
+
+// g[idx] = sum over chunks c = 0, 1, ... of part[c][idx] (a layer's W then b,
+// contiguous in the parameter layout).
+__global__ void mlp_sum_chunks_kernel(const float* __restrict__ part, uint32_t chunks, uint32_t n,
+                                      float* __restrict__ g) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  float acc = 0.f;
+  for (uint32_t c = 0; c < chunks; ++c) acc += part[(size_t)c * n + idx];
+  g[idx] = acc;
 }
 
 // Adam on the FP32 masters (bias-corrected), then the BF16 copy.
@@ -388,10 +404,12 @@ constexpr size_t kWorkPerRow = 4 * kH + kOut + 2 * kH + kOut + kIn + 2 + 1;
 struct Acts {
   float *Z1, *H1, *Z2, *H2, *Y, *dZ2, *dZ1, *dY, *bx, *bt;
   uint32_t* bm;
+  float* part;  // per-chunk partial weight gradients, ceil(B / kBwdChunk) x kMaxLayerParams
 };
 
 spx_status ensure_work(spx_ctx* ctx, spx_mlp* m, uint32_t B, Acts* a) {
-  const size_t need = (size_t)B * kWorkPerRow;
+  const size_t chunks = (B + kBwdChunk - 1) / kBwdChunk;
+  const size_t need = (size_t)B * kWorkPerRow + chunks * kMaxLayerParams;
   if (m->work_floats < need) {
     cudaError_t e = cudaSuccess;
     if (m->d_work) e = cudaStreamSynchronize(ctx->stream);
@@ -414,6 +432,7 @@ spx_status ensure_work(spx_ctx* ctx, spx_mlp* m, uint32_t B, Acts* a) {
   a->bx = a->dY + (size_t)B * kOut;
   a->bt = a->bx + (size_t)B * kIn;
   a->bm = reinterpret_cast<uint32_t*>(a->bt + (size_t)B * 2);
+  a->part = w + (size_t)B * kWorkPerRow;
   return SPX_OK;
 }
 
@@ -426,20 +445,29 @@ void forward(spx_ctx* ctx, spx_mlp* m, const float* X, uint32_t B, const Acts& a
   mlp_fwd_kernel<<<nblocks((uint64_t)B * kOut, 256), 256, 0, s>>>(a.H2, pb + kOffW3, p + kOffB3, B, kH, kOut, a.Y, nullptr, 0);
 }
 
-// Gradient of the masked MSE into m->d_g (zeroed first); loss accumulated into d_loss.
+// Weight and bias gradients of one layer (in -> out) into g (W then b),
+// through per-chunk partial sums added in a fixed order.
+void layer_weight_grad(cudaStream_t s, const float* dZ, const float* X, uint32_t B, int in, int out,
+                       const Acts& a, float* g) {
+  const unsigned ch = (B + kBwdChunk - 1) / kBwdChunk;
+  const uint32_t n = (uint32_t)(out * (in + 1));
+  mlp_bwd_weight_kernel<<<dim3(nblocks(n, 128), ch), 128, 0, s>>>(dZ, X, B, in, out, a.part);
+  mlp_sum_chunks_kernel<<<nblocks(n, 128), 128, 0, s>>>(a.part, ch, n, g);
+}
+
+// Gradient of the masked MSE into m->d_g (every entry written, the same bits
+// on every run); loss accumulated into d_loss.
 void backward(spx_ctx* ctx, spx_mlp* m, const float* X, const float* Tg, const uint32_t* mask,
               uint32_t B, const Acts& a, float* d_loss) {
   cudaStream_t s = ctx->stream;
   const __nv_bfloat16* pb = m->d_pb;
   float* g = m->d_g;
-  cudaMemsetAsync(g, 0, kNParams * sizeof(float), s);
   mlp_out_grad_kernel<<<nblocks((uint64_t)B * kOut, 256), 256, 0, s>>>(a.Y, Tg, mask, B, a.dY, d_loss);
-  const unsigned ch = (B + kBwdChunk - 1) / kBwdChunk;
-  mlp_bwd_weight_kernel<<<dim3(nblocks(kOut * (kH + 1), 128), ch), 128, 0, s>>>(a.dY, a.H2, B, kH, kOut, g + kOffW3, g + kOffB3);
+  layer_weight_grad(s, a.dY, a.H2, B, kH, kOut, a, g + kOffW3);
   mlp_bwd_data_kernel<<<nblocks((uint64_t)B * kH, 256), 256, 0, s>>>(a.dY, pb + kOffW3, a.Z2, B, kH, kOut, a.dZ2);
-  mlp_bwd_weight_kernel<<<dim3(nblocks(kH * (kH + 1), 128), ch), 128, 0, s>>>(a.dZ2, a.H1, B, kH, kH, g + kOffW2, g + kOffB2);
+  layer_weight_grad(s, a.dZ2, a.H1, B, kH, kH, a, g + kOffW2);
   mlp_bwd_data_kernel<<<nblocks((uint64_t)B * kH, 256), 256, 0, s>>>(a.dZ2, pb + kOffW2, a.Z1, B, kH, kH, a.dZ1);
-  mlp_bwd_weight_kernel<<<dim3(nblocks(kH * (kIn + 1), 128), ch), 128, 0, s>>>(a.dZ1, X, B, kIn, kH, g + kOffW1, g + kOffB1);
+  layer_weight_grad(s, a.dZ1, X, B, kIn, kH, a, g + kOffW1);
 }
 
 void adam(spx_ctx* ctx, spx_mlp* m, float lr) {
