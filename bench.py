@@ -46,6 +46,10 @@ METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima >
 # shows that the figure must be captured again.
 NCU_TRAFFIC_BYTES = 359_430_912
 NCU_TRAFFIC_KERNELS = {"kernels": ["fft_group_kernel<16384>", "maxima_cluster_kernel"], "commit": "ccafa54"}
+# What the ncu counters of the step's kernels show bounds them (same capture
+# as NCU_TRAFFIC_BYTES): neither DRAM nor the FP32 pipe is saturated.
+NCU_LIMITER = ("instruction issue and load latency: fft_group_kernel<16384> 41 % issue active, 13 % DRAM "
+               "throughput, 26 % FMA pipe, top stall long_scoreboard; maxima_cluster_kernel 19 % DRAM")
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
@@ -384,6 +388,18 @@ def run_gpu(args):
         line["workloads"] = workloads
     r = line["roofline"]
     r["frac"] = round(r["achieved"] / r["peak"], 4)
+    # The HBM fraction is small by construction (~85 FLOP per 8-byte sample):
+    # set beside it the nominal FFT work, 5 N log2 N flops per beam, against
+    # the FP32 CUDA-core peak (SMs x 128 lanes x 2 flops x max SM clock; the
+    # pool has no measured FP32 peak), and the limiter the ncu counters show.
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sms * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    flops = BEAMS * 5.0 * NFFT * np.log2(NFFT)
+    r["fp32"] = {"nominal_flops_per_step": flops, "achieved_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
+                 "peak_tflops": round(fp32_peak, 1), "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock",
+                 "frac": round(flops / (ms * 1e-3) / 1e12 / fp32_peak, 4)}
+    r["limiter"] = NCU_LIMITER
+    line["fp64"] = kern["fp64"]
     if args.cpu_sample_beams >= 0:
         v, cores, sample = cpu_measure(args.cpu_sample_beams or BEAMS, reps_budget_s=10.0)
         line["cpu_baseline"] = {"value": round(v, 3), "unit": "Msamples/s", "cores": cores, "kind": "port",
@@ -427,6 +443,10 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
         fused_ms.append(e0.elapsed_time(e1))
     f = statistics.median(fused_ms)
     n_max = int(counts.sum().item())
+    # FP64 error of the composed path's last spectrum (the fused path's transform is the same code)
+    xl = xs[(n - 1) % len(xs)]
+    pick = range(0, BEAMS, 32)
+    fp = fp64_error([xl[i].cpu().numpy() for i in pick], [spec[i].cpu().numpy() for i in pick], NFFT, WIN_HANN)
     # algorithmic bytes: samples read once + maxima and counts written
     algo = BEAMS * N_POINT * 8 + n_max * 32 + BEAMS * 4
     return {
@@ -445,6 +465,7 @@ def time_components(spx, ctx, xs, out, counts, p, stream, steps):
                      "algorithmic_bytes_per_launch": algo,
                      "maxima_per_launch": n_max},
         "launches_per_step": 2,
+        "fp64": fp,
     }
 
 
@@ -463,6 +484,37 @@ def _time_ms(stream, fn, reps):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     return statistics.median(ts)
+
+
+WIN_HANN, WIN_BH = 1, 4
+
+
+def _window64(kind: int, n: int) -> np.ndarray:
+    """The window in FP64 with the (n - 1) denominator (Hann, Blackman-Harris)."""
+    if n < 2:
+        return np.ones(n)
+    th = 2.0 * np.pi * np.arange(n) / (n - 1)
+    if kind == WIN_HANN:
+        return 0.5 - 0.5 * np.cos(th)
+    return 0.35875 - 0.48829 * np.cos(th) + 0.14128 * np.cos(2 * th) - 0.01168 * np.cos(3 * th)
+
+
+def fp64_error(xs, specs, nfft, kind) -> dict:
+    """Error of FP32 spectra against an FP64 FFT of the same FP32 samples
+    times the FP64 window: the largest max|dX| / max|X| and rms|dX| / max|X|
+    over the beams, and the smallest dynamic range max|X| / rms|dX|."""
+    mx, rms, dr = 0.0, 0.0, float("inf")
+    for x, sp in zip(xs, specs):
+        n = len(x)
+        X = np.fft.fft(x.astype(np.complex128) * _window64(kind, n), nfft or len(sp))
+        peak = float(np.abs(X).max())
+        e = np.abs(sp.astype(np.complex128) - X)
+        r = float(np.sqrt(np.mean(e ** 2)))
+        mx = max(mx, float(e.max()) / peak)
+        rms = max(rms, r / peak)
+        dr = min(dr, 20.0 * np.log10(peak / r) if r > 0 else 999.0)
+    return {"max_err_rel_peak": mx, "rms_err_rel_peak": rms, "dynamic_range_db": round(dr, 1),
+            "beams": len(xs), "reference": "numpy FFT in FP64 of the FP32 samples x FP64 window"}
 
 
 def bench_workloads(spx, ctx, stream, dev, hbm):
@@ -487,9 +539,11 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
     ms = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft_peaks(
         ctx.h, C.c_void_p(xs.data_ptr()), 8, 4096, 4096, spx.WINDOW_HANN, C.byref(p5),
         C.c_void_p(o5.data_ptr()), C.c_void_p(c5.data_ptr()))), 50)
+    spec_s = spx.fft(xs, 4096, window=spx.WINDOW_HANN).cpu().numpy()
     res["small"] = {"config": "8 x 4096, Hann, nFFT 4096, top-5, parabolic", "ms_per_step": round(ms, 4),
                     "Msamples_per_s": round(8 * 4096 / (ms * 1e-3) / 1e6, 1),
-                    "note": "launch-latency bound (one 8-CTA launch)"}
+                    "note": "launch-latency bound (one 8-CTA launch)",
+                    "fp64": fp64_error(list(xs.cpu().numpy()), list(spec_s), 4096, WIN_HANN)}
 
     # ---- uneven: 1024 beams, len U[1000, 100000], nFFT = next 2^a 3^b, top-8 ----
     bs = synth.workload_uneven(seed=2)
@@ -497,26 +551,69 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
     b = Batch(bs.lengths, window=spx.WINDOW_HANN, k=8, sample_rate=1.0, ctx=ctx)
     b.autotune(xu)
     ms_one = _time_ms(stream, lambda: b.run(xu), 20)
-    ms_per = _time_ms(stream, lambda: b.run_per_size(xu), 10)
+    ms_same_kernels = _time_ms(stream, lambda: b.run_per_size(xu), 10)
     side = torch.cuda.Stream(device=dev)   # graph capture needs a non-default stream
     with torch.cuda.stream(side):
         b.capture(xu, stream=side)
         ms_graph = _time_ms(side, lambda: b.replay(stream=side), 20)
     torch.cuda.synchronize()
     ctx.bind_stream(stream)
+    # the plain GPU path: every beam alone through spx_fft_peaks (its own
+    # window table, per-size FFT plan and kernels), as a caller of the
+    # per-size API runs it; eager, and the same calls captured in one graph
+    offs = np.concatenate([[0], np.cumsum(bs.lengths)]).astype(np.int64)
+    nffts_u = [spx.next_smooth23(int(v)) for v in bs.lengths]
+    pu = spx.peak_params(spx.PEAK_TOPK, 0, 0, 0, 8, spx.REFINE_PARABOLIC, 1.0, 0.0)
+    op = torch.zeros((bs.beams, 8, 8), dtype=torch.int32, device=dev)
+    cp = torch.zeros(bs.beams, dtype=torch.int32, device=dev)
+    calls = [(C.c_void_p(xu.data_ptr() + 8 * int(offs[i])), int(bs.lengths[i]), nffts_u[i],
+              C.c_void_p(op.data_ptr() + 256 * i), C.c_void_p(cp.data_ptr() + 4 * i)) for i in range(bs.beams)]
+    fpk, h, pref = spx.lib.spx_fft_peaks, ctx.h, C.byref(pu)
+
+    def plain_beams():
+        for a, n_, nf, o, c in calls:
+            fpk(h, a, 1, n_, nf, spx.WINDOW_HANN, pref, o, c)
+
+    ms_plain = _time_ms(stream, plain_beams, 3)
+    plain_same = bool(torch.equal(cp, b.counts) and torch.equal(op, b.out))
+    gph = torch.cuda.CUDAGraph()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        ctx.bind_stream(side)
+        with torch.cuda.graph(gph, stream=side, capture_error_mode="thread_local"):
+            plain_beams()
+        ms_plain_graph = _time_ms(side, gph.replay, 5)
+    torch.cuda.synchronize()
+    ctx.bind_stream(stream)
+    del gph
     samples = int(bs.lengths.sum())
-    algo_u = samples * 8 + 1024 * (8 * 32 + 4)
+    algo_u = samples * 8 + bs.beams * (8 * 32 + 4)
     best = min(ms_one, ms_graph)
+    # FP64 error of one beam of every distinct nFFT (the batch's spectra are these bits)
+    first = {}
+    for i, nf in enumerate(nffts_u):
+        first.setdefault(nf, i)
+    rows_x, rows_s = [], []
+    for i in sorted(first.values()):
+        beam = xu[offs[i]:offs[i + 1]].reshape(1, -1)
+        rows_x.append(beam.cpu().numpy()[0])
+        rows_s.append(spx.fft(beam, nffts_u[i], window=spx.WINDOW_HANN).cpu().numpy()[0])
     res["uneven"] = {"config": "1024 beams, n_point U[1000,100000], nFFT = next 2^a3^b, Hann, top-8",
-                     "samples": samples, "distinct_nfft": len({spx.next_smooth23(int(v)) for v in bs.lengths}),
+                     "samples": samples, "distinct_nfft": len(first),
                      "ms_one_launch": round(ms_one, 4), "ms_graph_replay": round(ms_graph, 4),
-                     "ms_per_size_plain": round(ms_per, 4),
+                     "ms_plain_per_beam_eager": round(ms_plain, 4),
+                     "ms_plain_per_beam_graph": round(ms_plain_graph, 4),
+                     "plain_path": "1024 spx_fft_peaks calls, one per beam (TOPK 8, Hann)",
+                     "plain_results_identical": plain_same,
+                     "speedup_vs_plain_graph": round(ms_plain_graph / best, 2),
+                     "speedup_vs_plain_eager": round(ms_plain / best, 2),
+                     "ms_batch_kernels_per_size": round(ms_same_kernels, 4),
                      "Msamples_per_s": round(samples / (best * 1e-3) / 1e6, 1),
-                     "speedup_vs_per_size": round(ms_per / best, 2),
                      "roofline": {"bound": "hbm", "achieved": round(algo_u / (best * 1e-3) / 1e9, 1),
                                   "peak": hbm, "unit": "GB/s",
-                                  "frac": round(algo_u / (best * 1e-3) / 1e9 / hbm, 4)}}
-    del xu, b
+                                  "frac": round(algo_u / (best * 1e-3) / 1e9 / hbm, 4)},
+                     "fp64": fp64_error(rows_x, rows_s, None, WIN_HANN)}
+    del xu, b, op, cp
 
     # ---- precision: 64 x 2^20, Blackman-Harris, two tones 120 dB apart ----
     n = 1 << 20
@@ -526,26 +623,14 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
     ms_fft = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft(
         ctx.h, C.c_void_p(xp.data_ptr()), 64, n, n, spx.WINDOW_BLACKMAN_HARRIS, spx.OUT_COMPLEX, 1.0,
         C.c_void_p(spec.data_ptr()))), 10)
-    # error against an FP64 transform of the same FP32 samples (two beams)
-    t = np.arange(n)
-    th = 2.0 * np.pi * t / (n - 1)
-    w = (0.35875 - 0.48829 * np.cos(th) + 0.14128 * np.cos(2 * th) - 0.01168 * np.cos(3 * th))
-    w = w.astype(np.float32).astype(np.float64)
-    errs_max, errs_rms, dr = [], [], []
-    for bb in (0, 63):
-        ref = np.fft.fft(xp[bb].cpu().numpy().astype(np.complex128) * w)
-        got = spec[bb].cpu().numpy().astype(np.complex128)
-        peak = np.abs(ref).max()
-        e = np.abs(got - ref)
-        errs_max.append(float(e.max() / peak))
-        rms = float(np.sqrt(np.mean(e ** 2)))
-        errs_rms.append(rms / peak)
-        dr.append(20 * np.log10(peak / rms))
+    # error against an FP64 transform of the same FP32 samples (four beams)
+    pb = (0, 21, 42, 63)
+    fp = fp64_error([xp[i].cpu().numpy() for i in pb], [spec[i].cpu().numpy() for i in pb], n, WIN_BH)
     res["precision"] = {"config": "64 x 2^20, Blackman-Harris, tones 120 dB apart + sigma 1e-7",
                         "ms_fft": round(ms_fft, 4),
                         "Msamples_per_s": round(64 * n / (ms_fft * 1e-3) / 1e6, 1),
-                        "max_rel_err_vs_fp64": max(errs_max), "rms_rel_err_vs_fp64": max(errs_rms),
-                        "dynamic_range_db": round(min(dr), 1), "beams_checked": [0, 63]}
+                        "max_rel_err_vs_fp64": fp["max_err_rel_peak"], "rms_rel_err_vs_fp64": fp["rms_err_rel_peak"],
+                        "dynamic_range_db": fp["dynamic_range_db"], "fp64": fp | {"beams_checked": list(pb)}}
     del xp, spec
 
     # ---- learned: train on 2^20 frames of 1024, infer on 4096 x 8192 ----
@@ -596,7 +681,9 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
                       "ms_refine_kernel": round(ms_kernel, 4),
                       "Msamples_per_s_with_refine": round(4096 * nl / (ms_ref * 1e-3) / 1e6, 1),
                       "freq_rms_bins_parabolic": round(rms_p, 6), "freq_rms_bins_learned": round(rms_m, 6),
-                      "rms_gain": round(rms_p / rms_m, 2)}
+                      "rms_gain": round(rms_p / rms_m, 2),
+                      "fp64": fp64_error([xl[i].cpu().numpy() for i in range(0, 4096, 256)],
+                                         [specl[i].cpu().numpy() for i in range(0, 4096, 256)], nl, WIN_HANN)}
     return res
 
 

@@ -51,32 +51,23 @@ struct BatchGeom {
   const float2* twc;
 };
 
-// Window value w[n] of an n_point-sample beam, evaluated on the fly (batches
-// have too many lengths for per-length tables): (n_point-1) denominator as
-// pad_data_windowed (fft_processor_kernels_rocm.hpp:97-110), cos via cospi.
-SPX_DEV float window_on_the_fly(uint32_t kind, uint32_t n, uint32_t n_point) {
-  if (kind == SPX_WINDOW_NONE || n_point < 2) return 1.0f;
-  const float t = __fdiv_rn(2.0f * (float)n, (float)(n_point - 1));  // theta / pi
-  const float c1 = cospif(t);
-  switch (kind) {
-    case SPX_WINDOW_HANN: return 0.5f - 0.5f * c1;
-    case SPX_WINDOW_HAMMING: return 0.54f - 0.46f * c1;
-    case SPX_WINDOW_BLACKMAN: return 0.42f - 0.5f * c1 + 0.08f * cospif(2.0f * t);
-    default:
-      return 0.35875f - 0.48829f * c1 + 0.14128f * cospif(2.0f * t) - 0.01168f * cospif(3.0f * t);
-  }
-}
-
+// Sample n of one beam of the batch: the window evaluated per sample by
+// window_at (the function that fills the per-size kernels' window tables, so
+// a batched beam and the same beam through spx_fft get the same windowed
+// bits), zero beyond n_point.
 struct SampleLoaderOTF {
   const float2* __restrict__ x;
-  uint32_t n_point, kind;
+  uint32_t n_point;
+  WindowGen wg;
   SPX_DEV float2 operator()(uint32_t n) const {
     float2 a = make_float2(0.f, 0.f);
     if (n < n_point) {
       a = ld_stream(x + n);
-      const float w = window_on_the_fly(kind, n, n_point);
-      a.x *= w;
-      a.y *= w;
+      if (wg.kind != SPX_WINDOW_NONE) {
+        const float w = window_at(wg, n);
+        a.x = __fmul_rn(a.x, w);
+        a.y = __fmul_rn(a.y, w);
+      }
     }
     return a;
   }
@@ -124,7 +115,7 @@ fft_batch_kernel(const float2* __restrict__ in, const BatchBeam* __restrict__ be
   const FftGeom& g = bg.g;
   const float2* twl = bg.twl;
   const float2* twc = bg.twc;
-  const SampleLoaderOTF ld{in + bm.in_off, bm.n_point, window};
+  const SampleLoaderOTF ld{in + bm.in_off, bm.n_point, make_window_gen(window, bm.n_point)};
   float2* slot = xch + bm.spec_off;
   if (active && g.C > 1) {
     switch (g.C) {

@@ -54,16 +54,112 @@ SPX_DEV float2 ld_stream(const float2* p) {
   return v;
 }
 
-// Sample n of a beam: window applied, zero beyond n_point.
+// ---- window ------------------------------------------------------------------
+// w[n], n < n_point, with the reference's (n_point - 1) denominator
+// (pad_data_windowed, include/spectrum/kernels/fft_processor_kernels_rocm.hpp:97-110),
+// c_k = cos(2 pi k n / (n_point - 1)):
+//   Hann 0.5 - 0.5 c1 (evaluated as sin^2(pi n / (n_point - 1)), the same
+//   value without the cancellation near the edges), Hamming 0.54 - 0.46 c1,
+//   Blackman 0.42 - 0.5 c1 + 0.08 c2,
+//   Blackman-Harris 0.35875 - 0.48829 c1 + 0.14128 c2 - 0.01168 c3.
+// This one FP32 evaluation is the window of every path: the window table of
+// the per-size kernels is filled by it on the device and the uneven batch
+// calls it per sample, so both apply the same bits and give the same spectra.
+// The argument is reduced exactly in integers: for an angle 2 pi m / D,
+// 4 m = q D + r gives the quadrant q and the angle (pi/2) r / D, which folds
+// to psi = (pi/2) s / D, s = min(r, D - r), psi in [0, pi/4]; (pi/2) / D is
+// carried as a sum of two floats, so psi is within an ulp.  cos and sin of
+// psi are their Taylor series (terms to psi^10 and psi^9; the first omitted
+// terms are below 1.2e-10 and 2.5e-9 on [0, pi/4]) in Horner form with explicit
+// FMAs, so no compiler contraction can change the bits.  Measured against
+// FP64: Hann within 3 ulps of w everywhere, every window within 1.2e-7
+// absolute (rounding the FP64 value to FP32 is within 3e-8).
+struct WindowGen {
+  uint32_t kind;   // spx_window (NONE when n_point < 2: w = 1)
+  uint32_t D;      // n_point - 1
+  float hi, lo;    // (pi/2) / D = hi + lo
+};
+
+SPX_DEV WindowGen make_window_gen(uint32_t kind, uint32_t n_point) {
+  constexpr float kPio2Hi = 1.57079637050628662f;     // pi/2 rounded to FP32
+  constexpr float kPio2Lo = -4.371139006309477e-8f;   // pi/2 - kPio2Hi
+  WindowGen g;
+  g.kind = n_point < 2 ? (uint32_t)SPX_WINDOW_NONE : kind;
+  g.D = n_point < 2 ? 1u : n_point - 1u;
+  const float d = __uint2float_rn(g.D);
+  g.hi = __fdiv_rn(kPio2Hi, d);
+  const float rem = __fmaf_rn(-g.hi, d, kPio2Hi);  // kPio2Hi - hi d, exact
+  g.lo = __fdiv_rn(__fadd_rn(rem, kPio2Lo), d);
+  return g;
+}
+
+// cos and sin of 2 pi m / D for m in [0, D), D < 2^29; (hi, lo) = (pi/2) / D.
+SPX_DEV float2 sincos_turn(uint32_t m, uint32_t D, float hi, float lo) {
+  const uint32_t m4 = 4u * m;
+  const uint32_t q = (uint32_t)(m4 >= D) + (uint32_t)(m4 >= 2u * D) + (uint32_t)(m4 >= 3u * D);
+  const uint32_t r = m4 - q * D;
+  const bool swap = 2u * r > D;
+  const float s = __uint2float_rn(swap ? D - r : r);
+  const float psi = __fmaf_rn(s, hi, __fmul_rn(s, lo));
+  const float y = __fmul_rn(psi, psi);
+  // cos psi = 1 - y/2 + y^2/24 - y^3/720 + y^4/40320 - y^5/3628800
+  float c = __fmaf_rn(y, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+  c = __fmaf_rn(c, y, -1.0f / 720.0f);
+  c = __fmaf_rn(c, y, 1.0f / 24.0f);
+  c = __fmaf_rn(c, y, -0.5f);
+  c = __fmaf_rn(c, y, 1.0f);
+  // sin psi = psi + psi y (-1/6 + y/120 - y^2/5040 + y^3/362880)
+  float p = __fmaf_rn(y, 1.0f / 362880.0f, -1.0f / 5040.0f);
+  p = __fmaf_rn(p, y, 1.0f / 120.0f);
+  p = __fmaf_rn(p, y, -1.0f / 6.0f);
+  const float sn = __fmaf_rn(__fmul_rn(psi, y), p, psi);
+  // angle = q pi/2 + phi, phi = psi (or pi/2 - psi when folded)
+  const float cphi = swap ? sn : c, sphi = swap ? c : sn;
+  const float cv = (q & 1u) ? sphi : cphi, sv = (q & 1u) ? cphi : sphi;
+  return make_float2((q == 1u || q == 2u) ? -cv : cv, (q >= 2u) ? -sv : sv);
+}
+
+// (k n) mod D for n <= D, k <= 3.
+SPX_DEV uint32_t mul_mod(uint32_t k, uint32_t n, uint32_t D) {
+  uint32_t m = k * n;
+  m = m >= D ? m - D : m;
+  m = m >= D ? m - D : m;
+  m = m >= D ? m - D : m;
+  return m;
+}
+
+SPX_DEV float cos_k(const WindowGen& g, uint32_t k, uint32_t n) {
+  return sincos_turn(mul_mod(k, n, g.D), g.D, g.hi, g.lo).x;
+}
+
+SPX_DEV float window_at(const WindowGen& g, uint32_t n) {
+  switch (g.kind) {
+    case SPX_WINDOW_HANN: {  // sin(2 pi n / (2D)); (pi/2) / (2D) = (hi + lo) / 2 exactly
+      const float s = sincos_turn(n, 2u * g.D, __fmul_rn(g.hi, 0.5f), __fmul_rn(g.lo, 0.5f)).y;
+      return __fmul_rn(s, s);
+    }
+    case SPX_WINDOW_HAMMING: return __fmaf_rn(-0.46f, cos_k(g, 1, n), 0.54f);
+    case SPX_WINDOW_BLACKMAN:
+      return __fmaf_rn(0.08f, cos_k(g, 2, n), __fmaf_rn(-0.5f, cos_k(g, 1, n), 0.42f));
+    case SPX_WINDOW_BLACKMAN_HARRIS:
+      return __fmaf_rn(-0.01168f, cos_k(g, 3, n),
+                       __fmaf_rn(0.14128f, cos_k(g, 2, n), __fmaf_rn(-0.48829f, cos_k(g, 1, n), 0.35875f)));
+    default: return 1.0f;
+  }
+}
+
+// Sample n of a beam: window applied (one rounded multiply per component,
+// never fused into the butterfly that follows: every path gets the same
+// windowed bits), zero beyond n_point.
 SPX_DEV float2 load_sample(const float2* __restrict__ x, uint32_t n,
                            uint32_t n_point, const float* __restrict__ win) {
   float2 a = make_float2(0.f, 0.f);
   if (n < n_point) {
     a = ld_stream(x + n);
     if (win) {
-      float w = __ldg(win + n);
-      a.x *= w;
-      a.y *= w;
+      const float w = __ldg(win + n);
+      a.x = __fmul_rn(a.x, w);
+      a.y = __fmul_rn(a.y, w);
     }
   }
   return a;

@@ -280,20 +280,12 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
   return SPX_OK;
 }
 
-// Window w[n], n < n_point, with the reference's (n_point - 1) denominator
-// (fft_processor_kernels_rocm.hpp:97-110), evaluated in FP64.
-static double window_value(uint32_t window, uint32_t n, uint32_t n_point) {
-  if (n_point < 2) return 1.0;
-  const double th = 2.0 * M_PI * (double)n / (double)(n_point - 1);
-  switch (window) {
-    case SPX_WINDOW_HANN: return 0.5 * (1.0 - std::cos(th));
-    case SPX_WINDOW_HAMMING: return 0.54 - 0.46 * std::cos(th);
-    case SPX_WINDOW_BLACKMAN: return 0.42 - 0.5 * std::cos(th) + 0.08 * std::cos(2.0 * th);
-    case SPX_WINDOW_BLACKMAN_HARRIS:
-      return 0.35875 - 0.48829 * std::cos(th) + 0.14128 * std::cos(2.0 * th) -
-             0.01168 * std::cos(3.0 * th);
-    default: return 1.0;
-  }
+// The window table of one (window, n_point): w[n] = window_at(n) (fft_core.cuh),
+// the evaluation the uneven batch makes per sample.
+__global__ void window_table_kernel(uint32_t window, uint32_t n_point, float* __restrict__ w) {
+  const WindowGen g = make_window_gen(window, n_point);
+  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < n_point; n += gridDim.x * blockDim.x)
+    w[n] = window_at(g, n);
 }
 
 spx_status get_window(spx_ctx* ctx, uint32_t window, uint32_t n_point, const float** out) {
@@ -309,15 +301,17 @@ spx_status get_window(spx_ctx* ctx, uint32_t window, uint32_t n_point, const flo
     *out = it->second;
     return SPX_OK;
   }
-  std::vector<float> w(n_point);
-  for (uint32_t n = 0; n < n_point; ++n) w[n] = (float)window_value(window, n, n_point);
   float* d = nullptr;
   cudaError_t e = cudaMalloc(&d, std::max<size_t>(1, n_point) * sizeof(float));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(window)");
-  e = cudaMemcpy(d, w.data(), n_point * sizeof(float), cudaMemcpyHostToDevice);
+  const uint32_t blocks = std::min<uint32_t>((n_point + 255) / 256, 4096);
+  window_table_kernel<<<std::max(blocks, 1u), 256, 0, ctx->stream>>>(window, n_point, d);
+  e = cudaGetLastError();
+  // filled once per (window, n_point); later calls may come on another stream
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(d);
-    return cuda_fail(ctx, e, "cudaMemcpy(window)");
+    return cuda_fail(ctx, e, "window table");
   }
   ctx->windows[key] = d;
   *out = d;
