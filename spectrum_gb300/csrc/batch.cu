@@ -419,7 +419,7 @@ spx_status build_launches(spx_ctx* ctx, spx_batch* b) {
 spx_status launch_set(spx_ctx* ctx, spx_batch* b, const LaunchSet& ls, const void* d_in,
                       spx_max_value* d_out, uint32_t* d_counts) {
   const void* kfn = ls.ept == 32 ? (const void*)fft_batch_kernel<32> : (const void*)fft_batch_kernel<16>;
-  cudaError_t e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
+  cudaError_t e = configure_kernel(kfn, kMaxFftSmem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_batch_kernel");
   const float2* in = static_cast<const float2*>(d_in);
   const BatchBeam* beams = b->d_beams;
@@ -562,7 +562,7 @@ spx_status spx_batch_capture(spx_ctx* ctx, spx_batch* batch, const void* d_in,
   // resolve lazy set-up before capturing
   cudaError_t e = configure_kernel(batch->ept == 32 ? (const void*)fft_batch_kernel<32>
                                                     : (const void*)fft_batch_kernel<16>,
-                                   kMaxLocal * sizeof(float2) + 16384);
+                                   kMaxFftSmem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_batch_kernel");
   e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamBeginCapture");

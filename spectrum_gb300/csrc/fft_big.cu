@@ -158,7 +158,7 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
   const void* kfn = (const void*)big_rows_kernel<kEPTDefault>;
-  e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
+  e = configure_kernel(kfn, kMaxFftSmem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows_kernel");
   FftGeom gg = g;
   gg.beams = beams;

@@ -16,8 +16,8 @@
 //   Z[k2] = X[k1 + C*k2] in natural order.
 // * C = 1: the first Stockham pass reads the samples from device memory.
 //
-// Shared memory layout: element i at sw(i) (spx_device.cuh), length
-// padded to a multiple of 16.  Twiddles are FP32 values of FP64-generated
+// Shared memory layout: element i at sw(i) (spx_device.cuh), sw_len(M)
+// elements per local FFT.  Twiddles are FP32 values of FP64-generated
 // exponentials: tw_local holds, per pass p with radix R and stride Ns,
 // W_{Ns R}^{r k} at [(r-1)*Ns + k] for r <= tw_rows(R) (radix 4: r = 1 only);
 // tw_cross holds W_N^{n2 k1} at [(k1-1)*M + n2].
@@ -422,9 +422,10 @@ SPX_DEV void p2_first(float2* s, const Load& load, uint32_t tid) {
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = load(j + r * B);
     Dft<R>::run(v);
-    const uint32_t lo = j & 15u, base = j * R;  // sw(base + r) = base + (r ^ lo) for R = 16; general below
+    // base = R j with R | 16: base mod 16 + r < 16, so sw(base + r) = sw(base) + r
+    const uint32_t sb = sw(j * R);
 #pragma unroll
-    for (int r = 0; r < R; ++r) s[R == 16 ? base + ((uint32_t)r ^ lo) : sw(base + r)] = v[r];
+    for (int r = 0; r < R; ++r) s[sb + r] = v[r];
   }
   __syncthreads();
 }
@@ -440,7 +441,7 @@ SPX_DEV void p2_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
     const uint32_t j = tid + q * T;
     const uint32_t sj = sw(j);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q][r] = s[(B % 256 == 0) ? sj + r * B : sw(j + r * B)];
+    for (int r = 0; r < R; ++r) v[q][r] = s[(B % 16 == 0) ? sj + sw(r * B) : sw(j + r * B)];
   }
   __syncthreads();
 #pragma unroll
@@ -459,7 +460,7 @@ SPX_DEV void p2_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
     const uint32_t base = (j - k) * R + k;
     const uint32_t sb = sw(base);
 #pragma unroll
-    for (int r = 0; r < R; ++r) s[(Ns % 256 == 0) ? sb + r * Ns : sw(base + r * Ns)] = v[q][r];
+    for (int r = 0; r < R; ++r) s[(Ns % 16 == 0) ? sb + sw(r * Ns) : sw(base + r * Ns)] = v[q][r];
   }
   __syncthreads();
 }

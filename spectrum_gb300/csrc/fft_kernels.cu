@@ -187,7 +187,7 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept, uint32_t pref_local) {
   r.nfft = nfft;
   r.C = C;
   r.M = nfft / C;
-  r.Mpad = (r.M + 15u) & ~15u;
+  r.Mpad = sw_len(r.M);
   uint32_t a = 0, b = 0, m = r.M;
   while (m % 2 == 0) { m /= 2; ++a; }
   while (m % 3 == 0) { m /= 3; ++b; }
@@ -387,7 +387,7 @@ uint32_t resident_beams(const void* kernel, const FftGeom& g, size_t smem) {
 template <typename K>
 static cudaError_t launch_beams(K kernel, FftGeom& g, uint32_t beams, size_t smem,
                                 cudaStream_t stream, void** args, bool prefetch) {
-  cudaError_t e0 = configure_kernel((const void*)kernel, kMaxLocal * sizeof(float2) + 16384);
+  cudaError_t e0 = configure_kernel((const void*)kernel, kMaxFftSmem);
   if (e0 != cudaSuccess) return e0;
   g.beams = beams;
   g.ahead = prefetch ? resident_beams((const void*)kernel, g, smem) : 0u;
@@ -440,7 +440,7 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     const void* kfn = g.M == 16384 ? (const void*)fft_group_out_kernel<16384>
                       : g.M == 8192 ? (const void*)fft_group_out_kernel<8192>
                                     : (const void*)fft_group_out_kernel<4096>;
-    e = configure_kernel(kfn, kMaxLocal * sizeof(float2) + 16384);
+    e = configure_kernel(kfn, kMaxFftSmem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "configure fft_group_out_kernel");
     uint32_t groups = resident_ctas(kfn, g.T, smem, 1) / g.C;  // all resident at once (cooperative)
     if (groups > beams) groups = beams;

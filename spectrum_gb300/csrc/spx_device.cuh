@@ -1,7 +1,7 @@
 // spx_device.cuh — device helpers shared by the FFT and peak kernels.
 //
 // Complex arithmetic on float2, register-resident forward DFTs of radix
-// 2/3/4/6/8/9/16 (natural order in and out), the shared-memory swizzle used
+// 2/3/4/6/8/9/16 (natural order in and out), the shared-memory layout used
 // by the Stockham passes, and the magnitude formula every kernel uses.
 #pragma once
 
@@ -39,13 +39,17 @@ SPX_DEV float2 mul_pos_i(float2 a) { return make_float2(-a.y, a.x); }  // a * (+
 SPX_DEV float mag2_rn(float2 z) { return __fadd_rn(__fmul_rn(z.x, z.x), __fmul_rn(z.y, z.y)); }
 SPX_DEV float mag_rn(float2 z) { return __fsqrt_rn(mag2_rn(z)); }
 
-// ---- shared-memory swizzle ---------------------------------------------------
-// Complex element i of a local FFT lives at sw(i).  XOR of bits 4..7 into
-// bits 0..3 keeps every aligned group of 16 elements in place, so arrays are
-// padded to a multiple of 16, and makes the stride-R stores of the first
-// Stockham pass (R = 8, 16) and the unit-stride loads of every pass
-// conflict-free for 64-bit accesses.
-SPX_DEV uint32_t sw(uint32_t i) { return i ^ ((i >> 4) & 15u); }
+// ---- shared-memory layout ------------------------------------------------------
+// Complex element i of a local FFT lives at sw(i) = i + floor(i / 16): one
+// unused element after every 16.  A half-warp's 64-bit accesses then hit 16
+// different bank pairs for unit strides (every pass's loads), for the stride-R
+// stores of a first Stockham pass (R = 2, 4, 8, 16) and for the stores of the
+// passes with a stride of 4 or 8.  For d a multiple of 16,
+// sw(i + d) = sw(i) + sw(d): strides that are multiples of 16 become constant
+// offsets, whatever the local size (power of two or 2^a 3^b).
+SPX_DEV uint32_t sw(uint32_t i) { return i + (i >> 4); }
+// Shared-memory elements of an n-point local FFT (n rounded up to 16).
+constexpr uint32_t sw_len(uint32_t n) { return ((n + 15u) & ~15u) + (((n + 15u) & ~15u) >> 4); }
 
 // ---- constants ---------------------------------------------------------------
 constexpr float kS2 = 0.70710678118654752440f;   // sqrt(1/2)

@@ -12,6 +12,9 @@ constexpr int kMaxPass = 12;
 constexpr uint32_t kMaxLocal = 16384;   // points per CTA (one local FFT)
 constexpr uint32_t kPrefLocalCluster = 16384;  // preferred points per CTA when C > 1 (measured fastest on GB300)
 constexpr int kEPTDefault = 16;         // points held per thread per pass (16 or 32)
+// Dynamic shared memory the FFT kernels may ask for: a padded 16384-point
+// local FFT (17408 elements) plus the fused kernels' histogram and lists.
+constexpr uint32_t kMaxFftSmem = (16384u + 1024u) * 8u + 32768u;
 
 // nfft = C * M.  The M-point local FFT runs npass Stockham passes; pass p
 // has radix radix[p], input stride ns[p] (product of earlier radices) and
@@ -26,7 +29,7 @@ struct FftGeom {
   uint32_t nfft;
   uint32_t C;       // CTAs per beam (cluster size)
   uint32_t M;       // local FFT length
-  uint32_t Mpad;    // M rounded up to a multiple of 16 (shared-memory elements)
+  uint32_t Mpad;    // shared-memory elements of the local FFT, sw_len(M) (spx_device.cuh)
   uint32_t T;       // threads per CTA
   uint32_t ept;     // points per thread (kernel instantiation: 16 or 32)
   uint32_t npass;
