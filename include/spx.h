@@ -300,23 +300,38 @@ spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
                               uint32_t* h_counts);
 
 /* ---- batches of uneven beams ---------------------------------------------
- * No reference counterpart (DspSpectrum transforms one nFFT per call).  A
- * batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->
+ * No reference counterpart (DspSpectrum transforms one nFFT per call; its
+ * nearest piece is host batching, src/fft_func/src/spectrum_processor_rocm.cpp:289-304).
+ * A batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->
  * spx_next_smooth23(n_point)), the window and TOPK peak parameters
- * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Every
- * nfft must run as one CTA or one cluster of at most 16 CTAs: 2^19 and
- * 2^20 (three-launch transforms) return SPX_ERR_UNSUPPORTED; run them
- * through spx_fft_peaks.  Inputs are
- * packed: beam i's samples start at sum_{j<i} n_point[j] (complex64); outputs
- * are [B x K] MaxValue and [B] counts.  Device scratch is owned by the batch.
- *  spx_batch_run           all beams in ONE FFT launch + one top-K launch
- *  spx_batch_run_per_size  the same kernels once per distinct nfft (the
+ * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Every nfft
+ * must run as C x M with C <= 16 CTAs of M <= 16384 points: 2^19 and 2^20
+ * (three-launch transforms) return SPX_ERR_UNSUPPORTED; run them through
+ * spx_fft_peaks.  Inputs are packed: beam i's samples start at
+ * sum_{j<i} n_point[j] (complex64); outputs are [B x K] MaxValue and [B]
+ * counts, each beam's list the bits spx_fft_peaks gives for that beam alone.
+ * Device scratch is owned by the batch.  A batch's plan for an nfft (its
+ * local size M, C = nfft / M) is the context's plan for that nfft: every
+ * call on the context uses it.
+ *  spx_batch_run           every beam's FFT in ONE launch (clusters of the
+ *                          largest C), then one top-K launch
+ *  spx_batch_run_per_size  the same kernel once per distinct nfft (the
  *                          per-size baseline; bit-identical results)
  *  spx_batch_capture/replay  record spx_batch_run for fixed pointers as a
  *                          CUDA graph on the context's (non-default) stream
- *  spx_batch_tune/autotune points per thread (16/32) and points per CTA of
- *                          clustered sizes; autotune times the candidates on
- *                          the given buffers and keeps the fastest */
+ *  spx_batch_tune          every size at the largest local size <= points_per_cta
+ *                          (points_per_thread must be 16)
+ *  spx_batch_local_size / spx_batch_set_local_size  one size's plan
+ *  spx_batch_autotune      per distinct nfft, times the whole batch on the
+ *                          given buffers with each candidate local size of that
+ *                          nfft and keeps the fastest (the current plan unless
+ *                          another is faster by over 2 %); *sizes_tuned = sizes
+ *                          with more than one candidate, *sizes_changed = plans
+ *                          changed
+ *  spx_batch_save_plans / spx_batch_load_plans  the plans as a JSON file
+ *                          {"arch": "sm_XY", "plans": {"<nfft>": M, ...}};
+ *                          loading applies the entries valid for the batch's
+ *                          sizes on a device of that architecture */
 typedef struct spx_batch spx_batch;
 spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_points,
                             const uint32_t* nffts, uint32_t window,
@@ -332,9 +347,15 @@ spx_status spx_batch_capture(spx_ctx* ctx, spx_batch* batch, const void* d_in,
 spx_status spx_batch_replay(spx_ctx* ctx, spx_batch* batch);
 spx_status spx_batch_tune(spx_ctx* ctx, spx_batch* batch, uint32_t points_per_thread,
                           uint32_t points_per_cta);
+uint32_t spx_batch_local_size(const spx_batch* batch, uint32_t nfft);
+spx_status spx_batch_set_local_size(spx_ctx* ctx, spx_batch* batch, uint32_t nfft,
+                                    uint32_t local_size);
 spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,
                               spx_max_value* d_out, uint32_t* d_counts,
-                              uint32_t* best_points_per_thread, uint32_t* best_points_per_cta);
+                              uint32_t* sizes_tuned, uint32_t* sizes_changed);
+spx_status spx_batch_save_plans(spx_ctx* ctx, const spx_batch* batch, const char* path);
+spx_status spx_batch_load_plans(spx_ctx* ctx, spx_batch* batch, const char* path,
+                                uint32_t* applied);
 
 /* ---- learned sub-bin refinement ------------------------------------------
  * No reference counterpart: it stands beside the 3-point parabola of

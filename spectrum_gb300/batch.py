@@ -2,9 +2,10 @@
 
     b = Batch(n_points, window=WINDOW_HANN, k=8, sample_rate=fs)
     out, counts = b.run(x_packed)            # one FFT launch + one top-K launch
-    out, counts = b.run_per_size(x_packed)   # one launch pair per distinct nfft
+    out, counts = b.run_per_size(x_packed)   # the same kernel once per distinct nfft
     b.capture(x_packed); b.replay()          # CUDA graph of run() for fixed buffers
-    b.autotune(x_packed)                     # pick points/thread and points/CTA
+    b.autotune(x_packed)                     # per-size local FFT sizes, timed
+    b.save_plans(path); b.load_plans(path)   # the plans as a JSON cache
 
 x_packed holds the beams back to back (complex64, sum(n_points) samples).
 """
@@ -38,6 +39,8 @@ class Batch:
                                             nf.ctypes.data_as(C.c_void_p) if nf is not None else None,
                                             window, C.byref(p), C.byref(h)))
         self.h = h
+        self.nffts = [int(nf[i]) if nf is not None and nf[i] else int(_capi.lib.spx_next_smooth23(int(v)))
+                      for i, v in enumerate(self.n_points)]
         dev = torch.device("cuda", self.ctx.device)
         self.out = torch.zeros((self.beams, self.k, 8), dtype=torch.int32, device=dev)
         self.counts = torch.zeros(self.beams, dtype=torch.int32, device=dev)
@@ -77,10 +80,34 @@ class Batch:
         self.ctx.check(lib.spx_batch_tune(self.ctx.h, self.h, points_per_thread, points_per_cta))
 
     def autotune(self, x):
-        e, p = C.c_uint32(), C.c_uint32()
+        """For every distinct nfft, times the whole batch with each candidate
+        local FFT size of that nfft and keeps the fastest; returns (sizes
+        tuned, plans changed)."""
+        t, c = C.c_uint32(), C.c_uint32()
         self.ctx.bind_stream()
-        self.ctx.check(lib.spx_batch_autotune(self.ctx.h, self.h, *self._args(x), C.byref(e), C.byref(p)))
-        return e.value, p.value
+        self.ctx.check(lib.spx_batch_autotune(self.ctx.h, self.h, *self._args(x), C.byref(t), C.byref(c)))
+        return t.value, c.value
+
+    def local_size(self, nfft: int) -> int:
+        """The local FFT size M of nfft's plan (C = nfft / M CTAs per beam)."""
+        return int(lib.spx_batch_local_size(self.h, int(nfft)))
+
+    def set_local_size(self, nfft: int, local_size: int):
+        self.ctx.check(lib.spx_batch_set_local_size(self.ctx.h, self.h, int(nfft), int(local_size)))
+
+    @property
+    def plans(self) -> dict:
+        """{nfft: local size} of the batch's distinct sizes."""
+        return {int(n): self.local_size(int(n)) for n in sorted(set(self.nffts))}
+
+    def save_plans(self, path):
+        self.ctx.check(lib.spx_batch_save_plans(self.ctx.h, self.h, str(path).encode()))
+
+    def load_plans(self, path) -> int:
+        """Applies a saved plan file; returns the number of entries applied."""
+        n = C.c_uint32()
+        self.ctx.check(lib.spx_batch_load_plans(self.ctx.h, self.h, str(path).encode(), C.byref(n)))
+        return n.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -392,104 +392,168 @@ SPX_DEV void local_passes(float2* s, const FftGeom& g, uint32_t p0,
 }
 
 // ---------------------------------------------------------------------------
-// Compile-time plans for power-of-two local sizes (EPT = 16).  The radix
-// order, strides and twiddle offsets are those build_geom emits for M = 2^a
-// (an 8 first when a = 3 mod 4, then 16s, then a 4 or a 2 last), so the
-// plan's twiddle table is used unchanged and the results are bit-identical to
-// the runtime passes; only the index arithmetic becomes constant.
+// Compile-time plans for local sizes M = 2^a 3^b <= 16384 (EPT = 16).  The
+// radix order, strides and twiddle offsets are those build_geom emits (an 8
+// first when a = 3 mod 4, then 16s, 9s, a 3 when b is odd, a 4 or 2 last),
+// so the plan's twiddle table is used unchanged and the results are
+// bit-identical to the runtime passes; only the index arithmetic becomes
+// constant.  The CTA has T threads (by default ceil(M / 16) rounded up to a
+// warp, the runtime plan's count): a pass of radix R has B = M / R
+// butterflies, Q = ceil(B / T) per thread, the last one guarded when T does
+// not divide B.  Which thread computes a butterfly does not change its
+// arithmetic, so any T gives the same bits.
 // ---------------------------------------------------------------------------
-constexpr int p2_log2(int x) { return x <= 1 ? 0 : 1 + p2_log2(x / 2); }
-template <int M>
-constexpr int p2_npass() { return p2_log2(M) / 4 + (p2_log2(M) % 4 ? 1 : 0); }
-template <int M>
-constexpr int p2_radix(int p) {
-  return p2_log2(M) % 4 == 3 ? (p == 0 ? 8 : 16)
-                             : (p < p2_log2(M) / 4 ? 16 : (p2_log2(M) % 4 == 2 ? 4 : 2));
-}
-template <int M>
-constexpr int p2_ns(int p) { return p == 0 ? 1 : p2_ns<M>(p - 1) * p2_radix<M>(p - 1); }
-template <int M>
-constexpr int p2_twoff(int p) { return p == 0 ? 0 : p2_twoff<M>(p - 1) + p2_ns<M>(p - 1) * (p2_radix<M>(p - 1) == 4 ? 1 : p2_radix<M>(p - 1) - 1); }
+constexpr int ct_v2(int m) { return m % 2 ? 0 : 1 + ct_v2(m / 2); }
+constexpr int ct_v3(int m) { return m % 3 ? 0 : 1 + ct_v3(m / 3); }
+constexpr int ct_pow3(int e) { return e == 0 ? 1 : 3 * ct_pow3(e - 1); }
 
-// First pass (Ns = 1) from device memory, M and the thread count T = M / 16 constant.
-template <int M, typename Load>
-SPX_DEV void p2_first(float2* s, const Load& load, uint32_t tid) {
-  constexpr int R = p2_radix<M>(0), T = M / 16, B = M / R, Q = 16 / R;
+template <int M>
+struct CtPlan {
+  static constexpr int a = ct_v2(M), b = ct_v3(M);
+  static constexpr bool lead8 = a % 4 == 3;
+  static constexpr int n16 = a / 4, n9 = b / 2, n3 = b % 2;
+  static constexpr int tail = lead8 ? 1 : (1 << (a % 4));  // last radix 2 or 4, 1 = none
+  static constexpr int npass = (lead8 ? 1 : 0) + n16 + n9 + n3 + (tail > 1 ? 1 : 0);
+  static constexpr int T = (((M + 15) / 16) + 31) / 32 * 32;
+  static constexpr int radix(int p) {
+    return lead8 && p == 0 ? 8
+         : (p - (lead8 ? 1 : 0)) < n16 ? 16
+         : (p - (lead8 ? 1 : 0) - n16) < n9 ? 9
+         : (p - (lead8 ? 1 : 0) - n16 - n9) < n3 ? 3
+         : tail;
+  }
+  static constexpr int ns(int p) { return p == 0 ? 1 : ns(p - 1) * radix(p - 1); }
+  static constexpr int twoff(int p) {
+    return p == 0 ? 0 : twoff(p - 1) + ns(p - 1) * (radix(p - 1) == 4 ? 1 : radix(p - 1) - 1);
+  }
+  static_assert(M == (1 << a) * ct_pow3(b) && M <= 16384, "M must be 2^a 3^b <= 16384");
+};
+
+// First pass (Ns = 1) from `load`, results into shared memory.
+template <int M, int T = CtPlan<M>::T, typename Load>
+SPX_DEV void ct_first(float2* s, const Load& load, uint32_t tid) {
+  using P = CtPlan<M>;
+  constexpr int R = P::radix(0), B = M / R, Q = (B + T - 1) / T;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const uint32_t j = tid + q * T;
-    float2 v[R];
+    if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
+      float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = load(j + r * B);
-    Dft<R>::run(v);
-    // base = R j with R | 16: base mod 16 + r < 16, so sw(base + r) = sw(base) + r
-    const uint32_t sb = sw(j * R);
+      for (int r = 0; r < R; ++r) v[r] = load(j + r * B);
+      Dft<R>::run(v);
+      if constexpr (16 % R == 0) {
+        // base = R j: base mod 16 + r < 16, so sw(base + r) = sw(base) + r
+        const uint32_t sb = sw(j * R);
 #pragma unroll
-    for (int r = 0; r < R; ++r) s[sb + r] = v[r];
+        for (int r = 0; r < R; ++r) s[sb + r] = v[r];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) s[sw(j * R + r)] = v[r];
+      }
+    }
   }
   __syncthreads();
 }
 
 // Pass P >= 1 in shared memory.
-template <int M, int P>
-SPX_DEV void p2_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
-  constexpr int R = p2_radix<M>(P), Ns = p2_ns<M>(P), T = M / 16, B = M / R, Q = 16 / R;
-  static_assert(Q * T * R == M, "every thread owns Q butterflies");
+template <int M, int P, int T>
+SPX_DEV void ct_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
+  using PL = CtPlan<M>;
+  constexpr int R = PL::radix(P), Ns = PL::ns(P), B = M / R, Q = (B + T - 1) / T;
   float2 v[Q][R];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const uint32_t j = tid + q * T;
-    const uint32_t sj = sw(j);
+    if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
+      const uint32_t sj = sw(j);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q][r] = s[(B % 16 == 0) ? sj + sw(r * B) : sw(j + r * B)];
+      for (int r = 0; r < R; ++r) v[q][r] = s[(B % 16 == 0) ? sj + sw(r * B) : sw(j + r * B)];
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const uint32_t j = tid + q * T;
-    const uint32_t k = j & (Ns - 1);
-    const float2* t = tw + p2_twoff<M>(P) + k;
-    if constexpr (R == 4) {
-      const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
-      v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
-    } else {
+    if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
+      const uint32_t k = j % Ns;
+      const float2* t = tw + PL::twoff(P) + k;
+      if constexpr (R == 4) {
+        const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
+        v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
+      } else {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+      }
+      Dft<R>::run(v[q]);
+      const uint32_t base = (j - k) * R + k;
+      const uint32_t sb = sw(base);
+#pragma unroll
+      for (int r = 0; r < R; ++r) s[(Ns % 16 == 0) ? sb + sw(r * Ns) : sw(base + r * Ns)] = v[q][r];
     }
-    Dft<R>::run(v[q]);
-    const uint32_t base = (j - k) * R + k;
-    const uint32_t sb = sw(base);
-#pragma unroll
-    for (int r = 0; r < R; ++r) s[(Ns % 16 == 0) ? sb + sw(r * Ns) : sw(base + r * Ns)] = v[q][r];
   }
   __syncthreads();
 }
 
-template <int M, int P>
-SPX_DEV void p2_passes_from(float2* s, const float2* __restrict__ tw, uint32_t tid) {
-  if constexpr (P < p2_npass<M>()) {
-    p2_pass<M, P>(s, tw, tid);
-    p2_passes_from<M, P + 1>(s, tw, tid);
+template <int M, int P, int T>
+SPX_DEV void ct_passes_from(float2* s, const float2* __restrict__ tw, uint32_t tid) {
+  if constexpr (P < CtPlan<M>::npass) {
+    ct_pass<M, P, T>(s, tw, tid);
+    ct_passes_from<M, P + 1, T>(s, tw, tid);
   }
 }
 
-// Whole local FFT of M points (first pass from `load`), M in {4096, 8192, 16384}.
-template <int M, typename Load>
-SPX_DEV void p2_local_fft(float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
-  p2_first<M>(s, load, tid);
-  p2_passes_from<M, 1>(s, tw, tid);
+// Whole local FFT of M points (first pass from `load`) by a CTA of T
+// threads, ending with a barrier.
+template <int M, int T = CtPlan<M>::T, typename Load>
+SPX_DEV void ct_local_fft(float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
+  ct_first<M, T>(s, load, tid);
+  ct_passes_from<M, 1, T>(s, tw, tid);
+}
+
+// The local sizes with an out-of-line compile-time plan (kernels that take
+// many sizes call them through ct_menu_fft; one register allocation each).
+// Together they cover every 2^a 3^b transform of 16385 .. 262144 points as
+// C x M with C in {2, 3, 4, 6, 8, 9, 12, 16}, each at the largest such M.
+template <int M, int T, typename Load>
+__device__ __noinline__ void ct_local_fft_ool(float2* s, Load load, const float2* __restrict__ tw, uint32_t tid) {
+  ct_local_fft<M, T>(s, load, tw, tid);
+}
+
+// The compile-time local FFT of M points when M is in the menu (returns
+// true), else nothing (returns false).  The CTA has T threads, or the plan's
+// default count when T = 0.
+template <int T, typename Load>
+SPX_DEV bool ct_menu_fft(uint32_t M, float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
+  switch (M) {
+    case 4096: ct_local_fft_ool<4096, T ? T : CtPlan<4096>::T>(s, load, tw, tid); return true;
+    case 5832: ct_local_fft_ool<5832, T ? T : CtPlan<5832>::T>(s, load, tw, tid); return true;
+    case 6144: ct_local_fft_ool<6144, T ? T : CtPlan<6144>::T>(s, load, tw, tid); return true;
+    case 6561: ct_local_fft_ool<6561, T ? T : CtPlan<6561>::T>(s, load, tw, tid); return true;
+    case 8192: ct_local_fft_ool<8192, T ? T : CtPlan<8192>::T>(s, load, tw, tid); return true;
+    case 8748: ct_local_fft_ool<8748, T ? T : CtPlan<8748>::T>(s, load, tw, tid); return true;
+    case 9216: ct_local_fft_ool<9216, T ? T : CtPlan<9216>::T>(s, load, tw, tid); return true;
+    case 10368: ct_local_fft_ool<10368, T ? T : CtPlan<10368>::T>(s, load, tw, tid); return true;
+    case 11664: ct_local_fft_ool<11664, T ? T : CtPlan<11664>::T>(s, load, tw, tid); return true;
+    case 12288: ct_local_fft_ool<12288, T ? T : CtPlan<12288>::T>(s, load, tw, tid); return true;
+    case 13122: ct_local_fft_ool<13122, T ? T : CtPlan<13122>::T>(s, load, tw, tid); return true;
+    case 13824: ct_local_fft_ool<13824, T ? T : CtPlan<13824>::T>(s, load, tw, tid); return true;
+    case 15552: ct_local_fft_ool<15552, T ? T : CtPlan<15552>::T>(s, load, tw, tid); return true;
+    case 16384: ct_local_fft_ool<16384, T ? T : CtPlan<16384>::T>(s, load, tw, tid); return true;
+    default: return false;
+  }
 }
 
 // Runs the local FFT with the compile-time plan when g is a power-of-two
-// size it covers (EPT 16, one thread per 16 points), else the runtime
+// size it covers inline (EPT 16, one thread per 16 points), else the runtime
 // plan.  Returns after the last pass's barrier either way.
 template <int EPT, typename Load>
 SPX_DEV void local_fft(float2* s, const FftGeom& g, const Load& load, const float2* __restrict__ tw,
                        uint32_t tid, uint32_t T) {
   if constexpr (EPT == 16) {
-    if (g.M == 16384 && T == 1024) return p2_local_fft<16384>(s, load, tw, tid);
-    if (g.M == 8192 && T == 512) return p2_local_fft<8192>(s, load, tw, tid);
-    if (g.M == 4096 && T == 256) return p2_local_fft<4096>(s, load, tw, tid);
+    if (g.M == 16384 && T == 1024) return ct_local_fft<16384>(s, load, tw, tid);
+    if (g.M == 8192 && T == 512) return ct_local_fft<8192>(s, load, tw, tid);
+    if (g.M == 4096 && T == 256) return ct_local_fft<4096>(s, load, tw, tid);
   }
   first_pass_dispatch<EPT>(s, g, load, tid, T);
   local_passes<EPT>(s, g, 1, tw, tid, T);

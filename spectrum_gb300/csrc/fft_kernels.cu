@@ -72,7 +72,8 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
   }
   cl.sync();
   float2* row = slot + (size_t)c * g.M;
-  local_fft<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T);
+  if (EPT != 16 || !ct_menu_fft<0>(g.M, s, ExchangeLoader{row}, tw_local, tid))
+    local_fft<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T);
   // row c was read by this CTA alone: it takes the CTA's spectrum row
   // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
   for (uint32_t i = tid; i < g.M; i += T) __stcg(row + i, s[sw(i)]);
@@ -110,7 +111,7 @@ fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
     }
     group_barrier(arrive + beam, g.C, err);
     float2* row = slot + (size_t)c * M;
-    p2_local_fft<M>(s, ExchangeLoader{row}, tw_local, tid);
+    ct_local_fft<M>(s, ExchangeLoader{row}, tw_local, tid);
     // row c was read by this CTA alone: it takes the CTA's spectrum row
     // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
     for (uint32_t i = tid; i < M; i += T) __stcg(row + i, s[sw(i)]);

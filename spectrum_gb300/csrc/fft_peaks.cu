@@ -350,7 +350,7 @@ fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
     if (beam + groups < g.beams) cross(beam + groups);
     group_wait(a.arrive + beam, g.C, a.err);
     float2* row = a.xch + (size_t)beam * g.nfft + (size_t)c * M;
-    p2_local_fft<M>(s, ExchangeLoader{row}, a.tw_local, tid);
+    ct_local_fft<M>(s, ExchangeLoader{row}, a.tw_local, tid);
     write_window_row(row, s, g, c, a.start, a.end, tid, T);
   }
 }

@@ -68,18 +68,47 @@ def test_batch_matches_oracle_without_window(spx, cuda):
         off += int(n)
 
 
-def test_batch_autotune_keeps_results(spx, cuda):
+def test_batch_autotune_keeps_results_and_plan_cache_round_trips(spx, cuda, tmp_path):
+    """The autotuner picks a local FFT size per distinct nfft by timing; any
+    choice gives the same lists bit for bit when the plain path uses the same
+    plan (the batch's plans are the context's).  A saved plan file loads back
+    into a new batch with the same plans and results."""
     import torch
     from spectrum_gb300.batch import Batch
-    n_points, x = _uneven(16, 1000, 40000, 13, extra=(80000,))
+    n_points, x = _uneven(16, 1000, 40000, 13, extra=(80000, 93312))
     xd = torch.from_numpy(x).to(cuda)
-    b = Batch(n_points, window=1, k=4)
+    ctx = spx.Context(0)
+    b = Batch(n_points, window=1, k=4, ctx=ctx)
     o1, c1 = [t.clone() for t in b.run(xd)]
-    ept, ppc = b.autotune(xd)
-    assert ept in (16, 32) and ppc in (8192, 16384)
-    o2, c2 = b.run(xd)
+    tuned, changed = b.autotune(xd)
+    assert tuned >= 2 and 0 <= changed <= tuned
+    o2, c2 = [t.clone() for t in b.run(xd)]
     np.testing.assert_array_equal(c1.cpu().numpy(), c2.cpu().numpy())
-    np.testing.assert_array_equal(spx.maxvalues_to_numpy(o1)["index"], spx.maxvalues_to_numpy(o2)["index"])
+    # every beam equals spx_fft_peaks on the same context (same plans)
+    g2 = spx.maxvalues_to_numpy(o2)
+    off = 0
+    for i, n in enumerate(n_points):
+        o, c = spx.fft_peaks(xd[off:off + int(n)].reshape(1, -1), b.nffts[i], 1, spx.PEAK_TOPK, sample_rate=1.0,
+                             max_per_beam=4, refine=spx.REFINE_PARABOLIC, ctx=ctx)
+        _same(spx.maxvalues_to_numpy(o)[0, :int(c[0])], g2[i, :int(c[0])])
+        off += int(n)
+    # force a different plan for 93312 = 6 x 15552 = 8 x 11664 and round-trip the cache
+    b.set_local_size(93312, 11664)
+    assert b.local_size(93312) == 11664
+    path = tmp_path / "plans.json"
+    b.save_plans(path)
+    assert '"93312": 11664' in path.read_text()
+    b2 = Batch(n_points, window=1, k=4, ctx=spx.Context(0))
+    assert b2.load_plans(path) == len(b.plans)
+    assert b2.plans == b.plans
+    o3, c3 = [t.clone() for t in b.run(xd)]
+    o4, c4 = [t.clone() for t in b2.run(xd)]
+    np.testing.assert_array_equal(c3.cpu().numpy(), c4.cpu().numpy())
+    _same(spx.maxvalues_to_numpy(o3), spx.maxvalues_to_numpy(o4))
+    with pytest.raises(ValueError):
+        b.set_local_size(93312, 1000)   # not C x M with C in the batch's cluster sizes
+    with pytest.raises(spx._capi.SpxError):
+        b.tune(32)                      # batches run 16 points per thread
 
 
 @pytest.mark.parametrize("n_point,nfft", [(500000, 0), (4096, 1 << 20)])
