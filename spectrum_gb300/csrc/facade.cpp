@@ -96,7 +96,7 @@ uint32_t checked_nfft(uint32_t n_point, uint32_t repeat_count, const char* where
   const uint64_t n = (uint64_t)spx_next_pow2(n_point) * repeat_count;
   if (n > 0xffffffffull || !spx_fft_size_supported((uint32_t)n))
     throw std::invalid_argument(std::string(where) + ": nFFT " + std::to_string(n) +
-                                " is not a transform size of this build (2^a 3^b <= 262144, 2^19, 2^20)");
+                                " is not a transform size of this build (any length 2 .. 2^20, or 2^21)");
   return (uint32_t)n;
 }
 

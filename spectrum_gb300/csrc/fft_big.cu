@@ -1,7 +1,8 @@
-// fft_big.cu — transforms of 2^19 and 2^20 points (the precision workload's
-// 2^20-point beams), beyond what one cluster holds on chip.
+// fft_big.cu — transforms of 2^19, 2^20 and 2^21 points (the precision
+// workload's 2^20-point beams; 2^21 = the reference's nextPow2(2^20) x
+// repeat_count 2), beyond what one cluster holds on chip.
 //
-// nfft = Cb * M with M = 16384 and Cb in {32, 64}; n = M*n1 + n2, k = k1 + Cb*k2:
+// nfft = Cb * M with M = 16384 and Cb in {32, 64, 128}; n = M*n1 + n2, k = k1 + Cb*k2:
 //   launch 1 (big_cols_kernel): for each n2, the Cb-point DFT over n1 of the
 //     windowed, zero-padded samples, times W_N^{n2 k1}, written to
 //     scratch[beam][k1][n2] (device memory);
@@ -52,7 +53,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
   }
   __syncthreads();
   const uint32_t col = tid & 31, t = tid >> 5;
-  constexpr int J = CB / 8;  // stage-1 radix (8 or 4)
+  constexpr int J = CB / 8;  // stage-1 radix (4, 8 or 16)
   // stage 1: thread t transforms rows t + 8j (j < J), twiddles W_CB^{t a}
   float2 v[J];
 #pragma unroll
@@ -67,17 +68,18 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
   for (int a = 0; a < J; ++a) tile[t + 8 * a][col] = v[a];
   __syncthreads();
-  // stage 2: for a = t (< J), the 8-point DFT over t' of rows t' + 8a -> k1 = a + J*b
-  if (t < (uint32_t)J) {
+  // stage 2: for a = t, t + 8, ... (< J), the 8-point DFT over t' of rows t' + 8a -> k1 = a + J*b
+#pragma unroll
+  for (uint32_t a = t; a < (uint32_t)J; a += 8) {
     float2 w[8];
 #pragma unroll
-    for (int tp = 0; tp < 8; ++tp) w[tp] = tile[tp + 8 * t][col];
+    for (int tp = 0; tp < 8; ++tp) w[tp] = tile[tp + 8 * a][col];
     Dft<8>::run(w);
     const uint32_t n2 = n2_0 + col;
     float2* o = scratch + (size_t)beam * nfft + n2;
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-      const uint32_t k1 = t + J * b;
+      const uint32_t k1 = a + J * b;
       o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + (size_t)k1 * kBigM + n2));  // W_N^{n2 k1}
     }
   }
@@ -97,7 +99,7 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, float2* __restri
   for (uint32_t i = tid; i < g.M; i += T) __stcs(row + i, s[sw(i)]);
 }
 
-bool big_size(uint32_t nfft) { return nfft == (1u << 19) || nfft == (1u << 20); }
+bool big_size(uint32_t nfft) { return nfft == (1u << 19) || nfft == (1u << 20) || nfft == (1u << 21); }
 
 // Geometry of the row FFTs (M = 16384, C = Cb as the output stride) and the
 // W_N table; called by get_plan for big sizes.
@@ -147,9 +149,13 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   if (st != SPX_OK) return st;
   float2* scratch = static_cast<float2*>(scr);
   dim3 grid(kBigM / 32, beams);
-  const void* kcols = g.C == 64 ? (const void*)big_cols_kernel<64> : (const void*)big_cols_kernel<32>;
+  const void* kcols = g.C == 128 ? (const void*)big_cols_kernel<128>
+                      : g.C == 64 ? (const void*)big_cols_kernel<64> : (const void*)big_cols_kernel<32>;
   const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, 256, 0, 1);
-  if (g.C == 64)
+  if (g.C == 128)
+    big_cols_kernel<128><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
+                                                        ahead_cols);
+  else if (g.C == 64)
     big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
                                                        ahead_cols);
   else

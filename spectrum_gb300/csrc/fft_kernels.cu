@@ -119,7 +119,7 @@ fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
 }
 
 // Bins k1 + C*q of the output from the row layout rows[beam][k1][q] (C rows
-// of M columns per beam, C <= 64): one CTA per `tc` columns of one beam; the
+// of M columns per beam, C <= 128): one CTA per `tc` columns of one beam; the
 // tile comes in along the rows (contiguous runs) and goes out in bin order
 // (contiguous runs in every output mode but the mirrored ones), through
 // shared memory with a row pitch of tc + 1 (conflict-free both ways).
@@ -231,6 +231,8 @@ static inline float2 twiddle(uint64_t m, uint64_t L) {
 FftPlan::~FftPlan() {
   if (d_tw_local) cudaFree(d_tw_local);
   if (d_tw_cross) cudaFree(d_tw_cross);
+  if (d_chirp) cudaFree(d_chirp);
+  if (d_bfft) cudaFree(d_bfft);
 }
 
 spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
@@ -251,9 +253,17 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
     ctx->plans.emplace(key, std::move(plan));
     return SPX_OK;
   }
-  if (!build_geom(nfft, &plan->g, ept, pref))
-    return fail(ctx, SPX_ERR_INVALID_ARG,
-                "nfft=" + std::to_string(nfft) + " is not a supported size (2^a*3^b up to 262144, or 2^19, 2^20)");
+  if (!build_geom(nfft, &plan->g, ept, pref)) {
+    if (!bluestein_size(nfft))
+      return fail(ctx, SPX_ERR_INVALID_ARG,
+                  "nfft=" + std::to_string(nfft) +
+                      " is not a supported size (2 .. 2^20 points, 2^a*3^b up to 262144, 2^21)");
+    spx_status st = build_bluestein_plan(ctx, nfft, plan.get());
+    if (st != SPX_OK) return st;
+    *out = plan.get();
+    ctx->plans.emplace(key, std::move(plan));
+    return SPX_OK;
+  }
   const FftGeom& g = plan->g;
   std::vector<float2> twl(std::max<uint32_t>(g.M, 1));
   for (uint32_t p = 0; p < g.npass; ++p) {
@@ -414,6 +424,7 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
                           uint32_t out_mode, float scale, void* d_out) {
   if (beams == 0) return SPX_OK;
   if (plan.big) return launch_fft_big(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
+  if (plan.bluestein) return launch_fft_bluestein(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
   FftGeom g = plan.g;
   const float2* twl = plan.d_tw_local;
   const float2* twc = plan.d_tw_cross;

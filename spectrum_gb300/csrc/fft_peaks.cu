@@ -405,7 +405,7 @@ struct MxArgs {
   float fs, factor;      // factor <= 0: no threshold
 };
 
-// Bin k of a beam's spectrum (offsets < nfft <= 2^20 fit 32 bits).
+// Bin k of a beam's spectrum (offsets < nfft <= 2^21 fit 32 bits).
 SPX_DEV float2 mx_load(const MxArgs& a, const float2* __restrict__ sb, uint32_t k) {
   uint32_t q, r;
   if (a.c1shift < 32) {

@@ -20,7 +20,14 @@ struct FftPlan {
   FftGeom g{};
   float2* d_tw_local = nullptr;  // M - 1 entries (>= 1 allocated)
   float2* d_tw_cross = nullptr;  // (C - 1) * M entries (big plans: W_N^{n2 k1} as [k1][n2], then W_Cb^e)
-  bool big = false;              // two-launch transform (2^19, 2^20 points)
+  bool big = false;              // three-launch transform (2^19, 2^20, 2^21 points)
+  // Sizes without a direct plan: Bluestein's chirp-z transform through a
+  // power-of-two transform of bm >= 2 nfft - 1 points (fft_bluestein.cu).
+  bool bluestein = false;
+  uint32_t bm = 0;
+  const FftPlan* sub = nullptr;  // the bm-point plan (owned by the context)
+  float2* d_chirp = nullptr;     // w[n] = exp(-i pi n^2 / nfft), n < nfft
+  float2* d_bfft = nullptr;      // FFT_bm of the conjugate chirp, wrapped
   ~FftPlan();
 };
 
@@ -42,8 +49,8 @@ struct spx_ctx {
   std::map<uint32_t, std::pair<uint32_t, uint32_t>> tuning;  // nfft -> (points/thread, points/CTA)
   std::map<uint64_t, float*> windows;  // (window << 32 | n_point) -> table
   // Grow-on-demand device scratch, one buffer per slot (see spx::Slot).
-  void* d_scratch[4] = {nullptr, nullptr, nullptr, nullptr};
-  size_t scratch_bytes[4] = {0, 0, 0, 0};
+  void* d_scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[5] = {0, 0, 0, 0, 0};
   uint32_t* d_error = nullptr;         // device error word (kErr* bits)
   uint32_t epoch = 0;                  // lookback status epoch
   // Host-buffer pipeline (spx_fft_peaks_host): copy streams, staging, events.
@@ -70,8 +77,10 @@ enum Slot : int {
   kSlotWork = 0,    // look-back status words, tickets, histograms
   kSlotThresh = 1,  // per-beam noise thresholds
   kSlotSpectrum = 2, // intermediate spectra of composed (non-fused) calls
-  kSlotExchange = 3  // per-cluster exchange slots of the large-FFT kernels
+  kSlotExchange = 3, // per-cluster exchange slots of the large-FFT kernels
+  kSlotChirp = 4     // the padded chirp-z sequences of Bluestein transforms
 };
+constexpr int kSlots = 5;
 // Ensures at least `bytes` in `slot`; returns its device pointer.  Growing a
 // slot frees the old buffer (cudaFree waits for the device first).
 spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
@@ -80,7 +89,14 @@ spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
 // up to 16) once per (device, kernel).
 cudaError_t configure_kernel(const void* kernel, size_t max_smem);
 
-// Two-launch transforms of 2^19 and 2^20 points (fft_big.cu).
+// Largest transform without a direct plan (Bluestein, through 2^21 points).
+constexpr uint32_t kMaxBluestein = 1u << 20;
+bool bluestein_size(uint32_t nfft);
+spx_status build_bluestein_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
+spx_status launch_fft_bluestein(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
+                                uint32_t n_point, const float* d_win, uint32_t out_mode, float scale,
+                                void* d_out);
+// Three-launch transforms of 2^19, 2^20 and 2^21 points (fft_big.cu).
 bool big_size(uint32_t nfft);
 spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
 spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,

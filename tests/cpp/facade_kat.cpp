@@ -402,8 +402,23 @@ static void gpufft_tests() {
   auto m2 = GpuFFT::Magnitude({{3.f, 4.f}}, true);
   check(m.size() == 2 && m[0] == 5.f && m[1] == 0.f && m2[0] == 25.f, "gpufft.magnitude");
   expect_throw<std::runtime_error>("gpufft.empty", [] { GpuFFT::ForwardC2C({}); });
-  expect_throw<std::invalid_argument>("gpufft.unsupported_length",
-                                      [] { GpuFFT::ForwardC2C(std::vector<std::complex<float>>(1000)); });
+  {  // CpuFFT takes any length: 1000 = 2^3 5^3 (Bluestein's transform on the GPU)
+    const uint32_t n1 = 1000;
+    std::vector<std::complex<float>> y(n1);
+    for (uint32_t t = 0; t < n1; ++t) y[t] = {std::cos(0.11f * t), std::sin(0.37f * t) + 0.2f};
+    auto Y = GpuFFT::ForwardC2C(y);
+    double e1 = 0.0, p1 = 0.0;
+    for (uint32_t k = 0; k < n1; ++k) {
+      std::complex<double> acc = 0.0;
+      for (uint32_t t = 0; t < n1; ++t) acc += std::complex<double>(y[t]) * std::polar(1.0, -2.0 * M_PI * k * t / n1);
+      e1 = std::max(e1, std::abs(acc - std::complex<double>(Y[k])));
+      p1 = std::max(p1, std::abs(acc));
+    }
+    check(Y.size() == n1 && e1 / p1 < 1e-5, "gpufft.any_length_1000", std::to_string(e1 / p1));
+  }
+  expect_throw<std::invalid_argument>("gpufft.unsupported_length", [] {
+    GpuFFT::ForwardC2C(std::vector<std::complex<float>>((1u << 20) + 1));
+  });
 }
 
 int main(int argc, char** argv) {

@@ -52,9 +52,12 @@ def test_next_smooth23_matches_oracle(lib):
 
 
 def test_fft_size_support(lib):
-    for n in (2, 3, 8, 4096, 13122, 59049, 104976, 131072, 262144, 1 << 19, 1 << 20):
+    """2^a 3^b sizes by the Stockham plans, 2^19 .. 2^21 by the three-launch
+    transform, every other length from 2 to 2^20 by Bluestein's transform."""
+    for n in (2, 3, 5, 7, 8, 1000, 1009, 4096, 13122, 59049, 104976, 131072, 262144, 524289, 3 << 18,
+              1 << 19, (1 << 20) - 1, 1 << 20, 1 << 21):
         assert lib.spx_fft_size_supported(n) == 1, n
-    for n in (0, 1, 5, 1000, 524289, 3 << 18, 1 << 21):
+    for n in (0, 1, (1 << 20) + 1, 3 << 20, 1 << 22):
         assert lib.spx_fft_size_supported(n) == 0, n
 
 

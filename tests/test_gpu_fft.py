@@ -23,6 +23,7 @@ FFT_CASES = [
     (17496, 17000, 0), (19683, 19683, 0), (32768, 20000, 1), (52488, 52000, 0),
     (65536, 65536, 3), (69984, 69000, 1), (104976, 100000, 1), (131072, 65536, 1),
     (59049, 59049, 0), (262144, 262144, 0), (1 << 19, 300000, 1), (1 << 20, 1 << 20, 4),
+    (1 << 21, 1 << 20, 1),  # nextPow2(2^20) x repeat_count 2, the reference's largest common FFTProcessor size
 ]
 
 
@@ -96,9 +97,9 @@ def test_fft_rejects_bad_sizes(spx, cuda):
     with pytest.raises(ValueError):
         spx.fft(x, 50)           # nfft < n_point
     with pytest.raises(ValueError):
-        spx.fft(x, 1000)         # 1000 = 2^3 * 5^3 is not 2^a 3^b
+        spx.fft(x, (1 << 20) + 1)  # beyond 2^20 only 2^21 (no direct plan, too long for Bluestein)
     with pytest.raises(ValueError):
-        spx.fft(x, 3 << 18)      # 2^18 * 3 exceeds the single-pass limit and is no two-launch size
+        spx.fft(x, 1 << 22)
 
 
 def test_precision_workload_dynamic_range(spx, cuda):
@@ -130,19 +131,46 @@ def _golden():
     return np.load(Path(__file__).parent / "golden" / "reference_golden.npz")
 
 
-@pytest.mark.parametrize("n", [64, 1000, 4096])
-def test_ifft_and_r2c_match_reference_cpufft(spx, cuda, n):
-    """Against the reference's own CpuFFT outputs (golden): 1e-5 of the peak.
-    CpuFFT takes any length; the GPU transforms take 2^a 3^b lengths and
-    reject others (1000 = 2^3 5^3) with SPX_ERR_INVALID_ARG."""
+@pytest.mark.parametrize("n", [64, 1000, 4096, 4374])
+def test_fft_any_length_matches_reference_cpufft(spx, cuda, n):
+    """CpuFFT::ForwardC2C takes any length; so does spx_fft up to 2^20 points
+    (1000 = 2^3 5^3 by Bluestein's transform, 4374 = 2 3^7 by the Stockham
+    plan): the reference's own outputs (golden) within 1e-5 of the peak."""
     import torch
     G = _golden()
-    if not spx.fft_size_supported(n):
-        with pytest.raises(ValueError):
-            spx.ifft(torch.from_numpy(G[f"ifft{n}_X"]).to(cuda))
-        with pytest.raises(ValueError):
-            spx.fft_r2c(torch.from_numpy(G[f"r2c{n}_x"]).to(cuda))
-        return
+    x, X = G[f"fft{n}_x"], G[f"fft{n}_X"]
+    got = spx.fft(torch.from_numpy(x).to(cuda), n).cpu().numpy()
+    assert np.abs(got - X).max() / np.abs(X).max() < FFT_TOL
+
+
+@pytest.mark.parametrize("nfft,n_point,win", [(5, 5, 0), (7, 6, 1), (1000, 900, 1), (1009, 1009, 4), (65537, 60000, 1),
+                                              ((1 << 20) - 1, 1 << 19, 2), (3 << 18, 700000, 0)])
+def test_bluestein_lengths_match_fp64(spx, cuda, nfft, n_point, win):
+    """Lengths without a Stockham plan (primes, 5- and 7-smooth, 2^20 - 1,
+    3 2^18): every output mode against the FP64 transform of the windowed,
+    zero-padded samples, within 1e-5 of the peak; the inverse round-trips."""
+    import torch
+    beams = 2 if nfft < (1 << 19) else 1
+    x = _signal(beams, n_point, nfft)
+    xd = torch.from_numpy(x).to(cuda)
+    ref = orc.fft_fp64(x, nfft, win)
+    got = spx.fft(xd, nfft, window=win).cpu().numpy()
+    peak = np.abs(ref).max()
+    assert np.abs(got - ref).max() / peak < FFT_TOL
+    mag = spx.fft(xd, nfft, window=win, out="mag").cpu().numpy()
+    assert np.abs(mag - np.abs(ref)).max() / peak < FFT_TOL
+    back = spx.ifft(spx.fft(xd, nfft)).cpu().numpy()
+    xp = np.zeros((beams, nfft), np.complex64)
+    xp[:, :n_point] = x
+    assert np.abs(back - xp).max() / np.abs(xp).max() < 1e-5
+
+
+@pytest.mark.parametrize("n", [64, 1000, 4096])
+def test_ifft_and_r2c_match_reference_cpufft(spx, cuda, n):
+    """Against the reference's own CpuFFT outputs (golden): 1e-5 of the peak,
+    at 2^a 3^b lengths and at 1000 = 2^3 5^3 (Bluestein's transform)."""
+    import torch
+    G = _golden()
     X, x = G[f"ifft{n}_X"], G[f"ifft{n}_x"]
     got = spx.ifft(torch.from_numpy(X).to(cuda)).cpu().numpy()
     assert np.abs(got - x).max() / np.abs(x).max() < FFT_TOL
@@ -158,7 +186,7 @@ def test_ifft_and_r2c_match_reference_cpufft(spx, cuda, n):
     np.testing.assert_array_equal(gf[:, : n // 2 + 1], gh)
 
 
-@pytest.mark.parametrize("nfft", [2, 9, 96, 4096, 13122, 65536, 131072, 1 << 20])
+@pytest.mark.parametrize("nfft", [2, 9, 96, 4096, 13122, 65536, 131072, 1 << 20, 1 << 21])
 def test_ifft_round_trip_and_fp64(spx, cuda, nfft):
     import torch
     beams = 2 if nfft < (1 << 20) else 1
