@@ -64,6 +64,8 @@ def _parse():
                     help="skip the small / uneven / precision / learned workload timings")
     ap.add_argument("--profile", action="store_true",
                     help="device steps only (warmup + steps), no timing report; for ncu captures")
+    ap.add_argument("--profile-beams", type=int, default=0,
+                    help="with --profile on the large workload: beams per step (0 = 256); full ncu captures use fewer")
     ap.add_argument("--profile-workload", default="large",
                     choices=["large", "plain4096", "plain16384", "uneven", "precision"],
                     help="with --profile: the fused large step, the plain FFT (|X|^2 out) of 16384 x 4096 or "
@@ -310,7 +312,8 @@ def run_gpu(args):
     # three rotating input buffers (different seeds) -> inputs larger than L2
     # (one buffer under --profile: fewer launches and less memory for ncu)
     nbuf = 1 if args.profile else 3
-    xs = [synth.synth_torch(synth.workload_large(seed=1 + 97 * rank + i, beams=BEAMS), device=dev)
+    nb = args.profile_beams if args.profile and args.profile_beams else BEAMS
+    xs = [synth.synth_torch(synth.workload_large(seed=1 + 97 * rank + i, beams=nb), device=dev)
           for i in range(nbuf)]
     torch.cuda.synchronize()
     _, _, cap = spx._capi.all_maxima_capacity(NFFT, 0, 0, 1000)
@@ -320,7 +323,7 @@ def run_gpu(args):
     p = spx.peak_params(spx.PEAK_ALL, 0, 0, 0, 1000, spx.REFINE_PARABOLIC, FS, SIGMA)
 
     def step(i):
-        ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(xs[i % nbuf].data_ptr()), BEAMS, N_POINT, NFFT,
+        ctx.check(spx.lib.spx_fft_peaks(ctx.h, C.c_void_p(xs[i % nbuf].data_ptr()), nb, N_POINT, NFFT,
                                         spx.WINDOW_HANN, C.byref(p), C.c_void_p(out.data_ptr()),
                                         C.c_void_p(counts.data_ptr())))
 
@@ -663,6 +666,9 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
                                          C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr()), None, None))
 
     ms_plain = _time_ms(stream, plain, 10)
+    ms_fused = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft_peaks(
+        ctx.h, C.c_void_p(xl.data_ptr()), 4096, nl, nl, spx.WINDOW_HANN, C.byref(p1), C.c_void_p(o1.data_ptr()),
+        C.c_void_p(c1.data_ptr()))), 10)
     ms_ref = _time_ms(stream, lambda: (plain(), refine_only()), 10)
     ms_kernel = _time_ms(stream, refine_only, 10)
     plain()
@@ -677,7 +683,8 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
                                 "20 epochs of 256 Adam steps; infer 4096 x 8192 at SNR 20 dB, top-1",
                       "make_frames_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
                       "final_loss": float(losses[-1]),
-                      "ms_plain_fft_topk": round(ms_plain, 4), "ms_with_learned_refine": round(ms_ref, 4),
+                      "ms_plain_fft_topk": round(ms_plain, 4), "ms_fused_fft_topk": round(ms_fused, 4),
+                      "ms_with_learned_refine": round(ms_ref, 4),
                       "ms_refine_kernel": round(ms_kernel, 4),
                       "Msamples_per_s_with_refine": round(4096 * nl / (ms_ref * 1e-3) / 1e6, 1),
                       "freq_rms_bins_parabolic": round(rms_p, 6), "freq_rms_bins_learned": round(rms_m, 6),

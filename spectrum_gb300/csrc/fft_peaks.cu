@@ -280,12 +280,14 @@ template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
 fft_peaks_kernel(FftGeom g, FusedArgs a) {
   extern __shared__ float2 s[];
-  // C == 1, after the spectrum: histogram / top-K lists [4096 + 64] | reductions [256]
-  uint32_t* shist = reinterpret_cast<uint32_t*>(s + g.Mpad);
-  uint32_t* s_red = shist + kHist + 64;
+  // C == 1, after the spectrum: histogram (with a threshold) or top-K lists
+  // [fused_extra_words - 256] | reductions [256]
   const uint32_t tid = threadIdx.x, T = blockDim.x;
+  uint32_t* shist = reinterpret_cast<uint32_t*>(s + g.Mpad);
+  uint32_t* s_red = shist + (a.factor > 0.0f ? kHist + 64 : 2 * T);
   if (g.C == 1) {
-    for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
+    if (a.factor > 0.0f)
+      for (uint32_t b = tid; b < kHist; b += T) shist[b] = 0;
     const uint32_t beam = blockIdx.x;
     prefetch_future_beam(g, a.in, a.n_point, beam, 0, tid, T);
     local_fft<EPT>(s, g, SampleLoader{a.in + (size_t)beam * a.n_point, a.n_point, a.win}, a.tw_local, tid, T);
@@ -614,9 +616,13 @@ maxima_cluster_kernel(MxArgs a) {
   }
 }
 
-// Shared memory of the fused kernel for geometry g.
-static size_t fused_smem(const FftGeom& g) {
-  return (size_t)g.Mpad * sizeof(float2) + (g.C == 1 ? (kHist + 64 + 256) * sizeof(uint32_t) : 0);
+// Shared memory of the fused kernel for geometry g: after the spectrum, with
+// a noise threshold the histogram (kHist + 64 words), else the top-K lists (a
+// 64-bit entry per thread), then 256 words of reductions.  Without the
+// threshold's 16 KB, an 8192-point beam's CTA fits three to an SM.
+static size_t fused_smem(const FftGeom& g, bool threshold = true) {
+  if (g.C != 1) return (size_t)g.Mpad * sizeof(float2);
+  return (size_t)g.Mpad * sizeof(float2) + ((threshold ? kHist + 64 : 2 * g.T) + 256) * sizeof(uint32_t);
 }
 
 // Cluster size and bins per CTA of maxima_cluster_kernel for a window of `span` bins.
@@ -710,7 +716,7 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
   a.refine = refine;
   a.fs = fs;
   a.factor = factor;
-  const size_t smem = fused_smem(g);
+  const size_t smem = fused_smem(g, factor > 0.0f);
   g.beams = beams;
   cudaError_t e;
   if (g.C == 1) {
