@@ -39,17 +39,19 @@ BEAMS, N_POINT, NFFT = 256, 65536, 131072
 FS = 1.0
 SIGMA = 6.0
 METRIC = "Msamples/s FFT+|X|+peaks (256x65536 -> nFFT 131072, Hann, all maxima > 6 sigma)"
-# DRAM bytes (read + write) of one step on this workload, the sum of
+# DRAM bytes (read + write) of one step on this workload: the sum of
 # dram__bytes_read.sum + dram__bytes_write.sum of fft_group_kernel<16384> and
-# maxima_cluster_kernel from one ncu capture; NCU_TRAFFIC_KERNELS names the
-# kernels it covers and the commit it was taken at, so a change of either
-# shows that the figure must be captured again.
-NCU_TRAFFIC_BYTES = 359_430_912
-NCU_TRAFFIC_KERNELS = {"kernels": ["fft_group_kernel<16384>", "maxima_cluster_kernel"], "commit": "ccafa54"}
+# maxima_cluster_kernel, one ncu capture of each on 160 beams, scaled by
+# 256 / 160 (every beam does the same work).  NCU_TRAFFIC_KERNELS names the
+# kernels and the commit the figure was taken at, so a change of either shows
+# that it must be captured again.
+NCU_TRAFFIC_BYTES = 355_558_195
+NCU_TRAFFIC_KERNELS = {"kernels": ["fft_group_kernel<16384>", "maxima_cluster_kernel"], "commit": "8e3509c",
+                       "beams_captured": 160}
 # What the ncu counters of the step's kernels show bounds them (same capture
 # as NCU_TRAFFIC_BYTES): neither DRAM nor the FP32 pipe is saturated.
-NCU_LIMITER = ("instruction issue and load latency: fft_group_kernel<16384> 41 % issue active, 13 % DRAM "
-               "throughput, 26 % FMA pipe, top stall long_scoreboard; maxima_cluster_kernel 19 % DRAM")
+NCU_LIMITER = ("instruction issue and load latency: fft_group_kernel<16384> 41 % issue active, 12.6 % DRAM "
+               "throughput, 26 % FMA pipe, top stall long_scoreboard; maxima_cluster_kernel 18.6 % DRAM")
 WORKLOAD = "plain-large: 256 beams x 65536 c64, Hann, nFFT 131072, all local maxima > 6 sigma, parabolic"
 
 
