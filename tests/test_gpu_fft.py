@@ -108,12 +108,12 @@ def test_precision_workload_dynamic_range(spx, cuda):
     spectrum's peak and the weak tone stands far above the error floor."""
     import torch
     from spectrum_gb300 import synth
-    bs = synth.workload_precision(seed=3, beams=2)
+    bs = synth.workload_precision(seed=3, beams=8)
     x = synth.synth_numpy(bs)
     n = 1 << 20
     got = spx.fft(torch.from_numpy(x).to(cuda), n, window=spx.WINDOW_BLACKMAN_HARRIS).cpu().numpy()
     ref = orc.fft_fp64(x, n, orc.WINDOW_BLACKMAN_HARRIS)
-    for b in range(2):
+    for b in range(8):
         peak = np.abs(ref[b]).max()
         err = np.abs(got[b] - ref[b])
         assert err.max() / peak < 1e-6, err.max() / peak
