@@ -276,11 +276,9 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(twiddles)");
   e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(twiddles)");
-  if (g.C > 1) {
-    std::vector<float2> twc((size_t)(g.C - 1) * g.M);
-    for (uint32_t k1 = 1; k1 < g.C; ++k1)
-      for (uint32_t n2 = 0; n2 < g.M; ++n2)
-        twc[(size_t)(k1 - 1) * g.M + n2] = twiddle((uint64_t)n2 * k1, g.nfft);
+  if (g.C > 1) {  // W_N^{n2}, n2 < M: the cross stage raises it to W_N^{n2 k1}
+    std::vector<float2> twc((size_t)g.M);
+    for (uint32_t n2 = 0; n2 < g.M; ++n2) twc[n2] = twiddle((uint64_t)n2, g.nfft);
     e = cudaMalloc(&plan->d_tw_cross, twc.size() * sizeof(float2));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(cross twiddles)");
     e = cudaMemcpy(plan->d_tw_cross, twc.data(), twc.size() * sizeof(float2), cudaMemcpyHostToDevice);

@@ -19,7 +19,7 @@ namespace spx {
 struct FftPlan {
   FftGeom g{};
   float2* d_tw_local = nullptr;  // M - 1 entries (>= 1 allocated)
-  float2* d_tw_cross = nullptr;  // (C - 1) * M entries (big plans: W_N^{n2 k1} as [k1][n2], then W_Cb^e)
+  float2* d_tw_cross = nullptr;  // W_N^{n2}, M entries (big plans: W_N^{n2 k1} as [k1][n2], then W_Cb^e)
   bool big = false;              // three-launch transform (2^19, 2^20, 2^21 points)
   // Sizes without a direct plan: Bluestein's chirp-z transform through a
   // power-of-two transform of bm >= 2 nfft - 1 points (fft_bluestein.cu).
