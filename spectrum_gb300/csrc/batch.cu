@@ -125,14 +125,13 @@ SPX_DEV void cross_otf(float2* slot, uint32_t c, uint32_t M, const SampleLoaderO
     for (int n1 = 0; n1 < CR; ++n1) v[n1] = ld(n1 * M + n2);
     Dft<CR>::run(v);
     __stcg(slot + n2, v[0]);
-    // W_N^{n2 k1} as successive products of W_N^{n2}, as cross_stage_exchange does
-    const float2 w1 = __ldg(twc + n2);
-    float2 w = w1;
+    // W_N^{n2 k1} by the product tree of cross_stage_exchange
+    float2 w[CR];
+    w[1] = __ldg(twc + n2);
 #pragma unroll
-    for (int k1 = 1; k1 < CR; ++k1) {
-      __stcg(slot + (size_t)k1 * M + n2, cmul(v[k1], w));
-      w = cmul(w, w1);
-    }
+    for (int k1 = 2; k1 < CR; ++k1) w[k1] = (k1 % 2 == 0) ? cmul(w[k1 / 2], w[k1 / 2]) : cmul(w[k1 - 1], w[1]);
+#pragma unroll
+    for (int k1 = 1; k1 < CR; ++k1) __stcg(slot + (size_t)k1 * M + n2, cmul(v[k1], w[k1]));
   }
 }
 
