@@ -397,12 +397,7 @@ def run_gpu(args):
     # set beside it the nominal FFT work, 5 N log2 N flops per beam, against
     # the FP32 CUDA-core peak (SMs x 128 lanes x 2 flops x max SM clock; the
     # pool has no measured FP32 peak), and the limiter the ncu counters show.
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    fp32_peak = sms * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
-    flops = BEAMS * 5.0 * NFFT * np.log2(NFFT)
-    r["fp32"] = {"nominal_flops_per_step": flops, "achieved_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
-                 "peak_tflops": round(fp32_peak, 1), "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock",
-                 "frac": round(flops / (ms * 1e-3) / 1e12 / fp32_peak, 4)}
+    r["fp32"] = fp32_figure(BEAMS * 5.0 * NFFT * np.log2(NFFT), ms, dev)
     r["limiter"] = NCU_LIMITER
     line["fp64"] = kern["fp64"]
     if args.cpu_sample_beams >= 0:
@@ -502,6 +497,20 @@ def _window64(kind: int, n: int) -> np.ndarray:
     if kind == WIN_HANN:
         return 0.5 - 0.5 * np.cos(th)
     return 0.35875 - 0.48829 * np.cos(th) + 0.14128 * np.cos(2 * th) - 0.01168 * np.cos(3 * th)
+
+
+def fp32_figure(flops: float, ms: float, dev) -> dict:
+    """Nominal FFT work (5 N log2 N flops per transform) per step against the
+    FP32 CUDA-core peak (SMs x 128 lanes x 2 flops x max SM clock; the pool
+    has no measured FP32 peak)."""
+    import torch
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = sms * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    got = flops / (ms * 1e-3) / 1e12
+    return {"nominal_flops_per_step": flops, "achieved_tflops": round(got, 2), "peak_tflops": round(peak, 1),
+            "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock", "frac": round(got / peak, 4)}
 
 
 def fp64_error(xs, specs, nfft, kind) -> dict:
@@ -616,7 +625,8 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
                      "Msamples_per_s": round(samples / (best * 1e-3) / 1e6, 1),
                      "roofline": {"bound": "hbm", "achieved": round(algo_u / (best * 1e-3) / 1e9, 1),
                                   "peak": hbm, "unit": "GB/s",
-                                  "frac": round(algo_u / (best * 1e-3) / 1e9 / hbm, 4)},
+                                  "frac": round(algo_u / (best * 1e-3) / 1e9 / hbm, 4),
+                                  "fp32": fp32_figure(sum(5.0 * nf * np.log2(nf) for nf in nffts_u), best, dev)},
                      "fp64": fp64_error(rows_x, rows_s, None, WIN_HANN)}
     del xu, b, op, cp
 
