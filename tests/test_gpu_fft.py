@@ -124,6 +124,48 @@ def test_precision_workload_dynamic_range(spx, cuda):
         assert 20 * np.log10(weak_mag / rms) > 40       # the -120 dB tone is visible
 
 
+BIN_REL_TOL = 1e-5
+
+
+@pytest.mark.parametrize("workload", ["small", "large", "uneven", "precision", "learned"])
+def test_magnitude_per_bin_relative_error(spx, cuda, workload):
+    """|X| per bin within 1e-5 relative of pocketfft's FP32 |X| and of the
+    FP64 |X|, on every bin 20 dB or more above the beam's median |X| (the
+    noise floor) and within 60 dB of its peak, for beams of each benchmark
+    workload.  (The whole-spectrum bound above is 1e-5 of the beam's peak.)"""
+    import torch
+    from spectrum_gb300 import synth
+    win = spx.WINDOW_BLACKMAN_HARRIS if workload == "precision" else spx.WINDOW_HANN
+    if workload == "small":
+        bs, rows = synth.workload_small(seed=0), range(8)
+    elif workload == "large":
+        bs, rows = synth.workload_large(seed=1, beams=4), range(4)
+    elif workload == "uneven":
+        bs, rows = synth.workload_uneven(seed=2, beams=64), range(0, 64, 8)
+    elif workload == "precision":
+        bs, rows = synth.workload_precision(seed=3, beams=2), range(2)
+    else:
+        bs, rows = synth.workload_learned(seed=4, beams=8), range(8)
+    xs = synth.synth_numpy(bs)
+    checked = 0
+    for b in rows:
+        n = int(bs.lengths[b])
+        x = np.ascontiguousarray(xs[b:b + 1, :n])
+        nfft = {"small": 4096, "large": 131072, "precision": 1 << 20, "learned": 8192}.get(
+            workload, orc.next_smooth23(n))
+        got = np.abs(spx.fft(torch.from_numpy(x).to(cuda), nfft, window=win).cpu().numpy()[0]).astype(np.float64)
+        a64 = np.abs(orc.fft_fp64(x, nfft, win)[0])
+        a32 = np.abs(orc.fft_fp32(x, nfft, win)[0]).astype(np.float64)
+        sel = (a64 >= 10.0 * np.median(a64)) & (a64 >= 1e-3 * a64.max())
+        assert sel.sum() > 0
+        r64 = float((np.abs(got[sel] - a64[sel]) / a64[sel]).max())
+        r32 = float((np.abs(got[sel] - a32[sel]) / a32[sel]).max())
+        assert r64 < BIN_REL_TOL, f"beam {b}: {r64:.3e} vs FP64"
+        assert r32 < BIN_REL_TOL, f"beam {b}: {r32:.3e} vs FP32 pocketfft"
+        checked += int(sel.sum())
+    assert checked >= 10
+
+
 # ---- inverse and real-input transforms (CpuFFT::InverseC2C / ForwardR2C / ForwardR2C_Full) ----
 
 def _golden():
