@@ -415,9 +415,10 @@ class SpectrumProcessorFactory {
 // ---------------------------------------------------------------------------
 // CpuFFT's static API (include/spectrum/utils/cpu_fft.hpp:68-203) computed on
 // GPU 0: host vectors in and out, one transform per call.  Any length from
-// 2 to 2^20 (2^a 3^b lengths by the Stockham plans, others by Bluestein's
-// chirp-z transform), or 2^21: std::invalid_argument otherwise; an empty
-// input throws std::runtime_error as CpuFFT does.
+// 2 to 2^27 (2^a 3^b lengths by the Stockham and four-step plans, others by
+// Bluestein's chirp-z transform), and 2^a 3^b lengths up to 2^28 that split
+// into two factors <= 16384: std::invalid_argument otherwise; an empty input
+// throws std::runtime_error as CpuFFT does.
 // ---------------------------------------------------------------------------
 namespace spectrum_utils {
 

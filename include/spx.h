@@ -166,8 +166,12 @@ spx_status spx_selftest_group_wait_timeout(spx_ctx* ctx);
 uint32_t spx_next_pow2(uint32_t n);
 /* Smallest 2^a*3^b >= n (extension for beams of uneven length). */
 uint32_t spx_next_smooth23(uint32_t n);
-/* 1 if this build can transform nfft points: 2^a*3^b in [2, 262144] in one
- * pass (cluster of <= 16 CTAs), or 2^19 / 2^20 in two launches; else 0. */
+/* 1 if this build can transform nfft points; else 0.  2^a*3^b in
+ * [2, 262144]: one pass (cluster of <= 16 CTAs); 2^19 .. 2^21: three
+ * launches; 2^a*3^b above 2^21 up to 2^28 that split into two factors
+ * <= 16384 (every power of two): four steps with transposes; any other
+ * length up to 2^27: Bluestein's chirp-z transform.  The reference takes any
+ * nextPow2(n_point) * repeat_count (fft_processor_rocm.cpp:673-677). */
 int spx_fft_size_supported(uint32_t nfft);
 /* Tuning for transforms of nfft points: points each thread holds per pass
  * (16: more resident warps; 32: more work per thread) and, above 16384
@@ -305,9 +309,9 @@ spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
  * A batch fixes B beams with their own n_point and nfft (nffts NULL or 0 ->
  * spx_next_smooth23(n_point)), the window and TOPK peak parameters
  * (params->mode must be SPX_PEAK_TOPK, K <= 32, thresh_sigma 0).  Every nfft
- * must run as C x M with C <= 16 CTAs of M <= 16384 points: 2^19 and 2^20
- * (three-launch transforms) return SPX_ERR_UNSUPPORTED; run them through
- * spx_fft_peaks.  Inputs are packed: beam i's samples start at
+ * must run as C x M with C <= 16 CTAs of M <= 16384 points: 2^19 points
+ * and more (multi-launch transforms) return SPX_ERR_UNSUPPORTED; run them
+ * through spx_fft_peaks.  Inputs are packed: beam i's samples start at
  * sum_{j<i} n_point[j] (complex64); outputs are [B x K] MaxValue and [B]
  * counts, each beam's list the bits spx_fft_peaks gives for that beam alone.
  * Device scratch is owned by the batch.  A batch's plan for an nfft (its

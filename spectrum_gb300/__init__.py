@@ -118,6 +118,8 @@ def fft(x, nfft: int | None = None, window: int = WINDOW_NONE, out: str = "compl
     beams, n_point = x2.shape
     nfft = int(nfft or n_point)
     mode = _OUT_MODES[out]
+    if not 0 < nfft <= 0xFFFFFFFF or not lib.spx_fft_size_supported(nfft):
+        raise ValueError(f"spx_fft: nfft={nfft} is not a transform size of this build")
     shape = (beams, nfft)
     if mode == OUT_COMPLEX:
         o = torch.empty(shape, dtype=torch.complex64, device=x.device)

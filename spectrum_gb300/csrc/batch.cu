@@ -596,11 +596,11 @@ spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_poin
       return fail(ctx, SPX_ERR_INVALID_ARG,
                   "spx_batch_create: beam " + std::to_string(i) + " has an unsupported size");
     }
-    if (big_size(n)) {  // three-launch transforms: not slots of the batch kernel
+    if (big_size(n) || huge_size(n)) {  // multi-launch transforms: not slots of the batch kernel
       delete b;
       return fail(ctx, SPX_ERR_UNSUPPORTED,
                   "spx_batch_create: beam " + std::to_string(i) + " needs nfft " + std::to_string(n) +
-                      "; 2^19 and 2^20 points run through spx_fft_peaks, not in a batch");
+                      "; transforms of 2^19 points and more run through spx_fft_peaks, not in a batch");
     }
     b->nfft[i] = n;
     if (!b->local.count(n)) {

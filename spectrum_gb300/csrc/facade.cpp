@@ -96,7 +96,8 @@ uint32_t checked_nfft(uint32_t n_point, uint32_t repeat_count, const char* where
   const uint64_t n = (uint64_t)spx_next_pow2(n_point) * repeat_count;
   if (n > 0xffffffffull || !spx_fft_size_supported((uint32_t)n))
     throw std::invalid_argument(std::string(where) + ": nFFT " + std::to_string(n) +
-                                " is not a transform size of this build (any length 2 .. 2^20, or 2^21)");
+                                " is not a transform size of this build (any length 2 .. 2^27; 2^a 3^b up to 2^28"
+                                " with a split into two factors <= 16384)");
   return (uint32_t)n;
 }
 
@@ -834,31 +835,40 @@ std::vector<Out> run(const std::vector<In>& input, size_t out_len, const char* w
   return r;
 }
 
+// The transform size of an input of `len` elements, rejected before any
+// device memory is taken when this build has no transform of that length.
+uint32_t transform_len(size_t len, const char* where) {
+  if (len > 0 && (len > 0xffffffffull || !spx_fft_size_supported((uint32_t)len)))
+    throw std::invalid_argument(std::string("GpuFFT::") + where + ": length " + std::to_string(len) +
+                                " is not a transform size of this build");
+  return (uint32_t)len;
+}
+
 }  // namespace
 
 std::vector<std::complex<float>> GpuFFT::ForwardC2C(const std::vector<std::complex<float>>& input) {
-  const uint32_t n = (uint32_t)input.size();
+  const uint32_t n = transform_len(input.size(), "ForwardC2C");
   return run<std::complex<float>, std::complex<float>>(input, n, "ForwardC2C", [n](spx_ctx* c, const void* i, void* o) {
     return spx_fft(c, i, 1, n, n, SPX_WINDOW_NONE, SPX_OUT_COMPLEX, 1.0f, o);
   });
 }
 
 std::vector<std::complex<float>> GpuFFT::InverseC2C(const std::vector<std::complex<float>>& input) {
-  const uint32_t n = (uint32_t)input.size();
+  const uint32_t n = transform_len(input.size(), "InverseC2C");
   return run<std::complex<float>, std::complex<float>>(input, n, "InverseC2C", [n](spx_ctx* c, const void* i, void* o) {
     return spx_ifft(c, i, 1, n, o);
   });
 }
 
 std::vector<std::complex<float>> GpuFFT::ForwardR2C(const std::vector<float>& input) {
-  const uint32_t n = (uint32_t)input.size();
+  const uint32_t n = transform_len(input.size(), "ForwardR2C");
   return run<float, std::complex<float>>(input, n / 2 + 1, "ForwardR2C", [n](spx_ctx* c, const void* i, void* o) {
     return spx_fft_r2c(c, static_cast<const float*>(i), 1, n, n, SPX_WINDOW_NONE, 0, o);
   });
 }
 
 std::vector<std::complex<float>> GpuFFT::ForwardR2C_Full(const std::vector<float>& input) {
-  const uint32_t n = (uint32_t)input.size();
+  const uint32_t n = transform_len(input.size(), "ForwardR2C_Full");
   return run<float, std::complex<float>>(input, n, "ForwardR2C_Full", [n](spx_ctx* c, const void* i, void* o) {
     return spx_fft_r2c(c, static_cast<const float*>(i), 1, n, n, SPX_WINDOW_NONE, 1, o);
   });

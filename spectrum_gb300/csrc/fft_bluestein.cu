@@ -1,11 +1,11 @@
 // fft_bluestein.cu — transforms of any length without a direct plan (not
-// 2^a 3^b, e.g. 1000 = 2^3 5^3 or a prime), up to 2^20 points.
+// 2^a 3^b, e.g. 1000 = 2^3 5^3 or a prime), up to 2^27 points.
 //
 // The reference's CpuFFT takes any length (pocketfft,
 // include/spectrum/utils/cpu_fft.hpp:68-89); this is the GPU counterpart for
 // the lengths the Stockham plans do not cover.  Bluestein's chirp-z identity
 // n k = (n^2 + k^2 - (k - n)^2) / 2 turns the N-point DFT into a circular
-// convolution of length m >= 2N - 1 (a power of two, m <= 2^21):
+// convolution of length m >= 2N - 1 (a power of two, m <= 2^28):
 //   w[n] = exp(-i pi n^2 / N)
 //   X[k] = w[k] * sum_n (x[n] w[n]) conj(w[k - n])
 //        = w[k] * IFFT_m( FFT_m(a) * FFT_m(b) )[k],
@@ -27,7 +27,7 @@ namespace spx {
 
 bool bluestein_size(uint32_t nfft) {
   FftGeom g;
-  return nfft >= 2 && nfft <= kMaxBluestein && !build_geom(nfft, &g) && !big_size(nfft);
+  return nfft >= 2 && nfft <= kMaxBluestein && !build_geom(nfft, &g) && !big_size(nfft) && !huge_size(nfft);
 }
 
 static uint32_t bluestein_m(uint32_t nfft) {

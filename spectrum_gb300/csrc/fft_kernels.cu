@@ -253,11 +253,19 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
     ctx->plans.emplace(key, std::move(plan));
     return SPX_OK;
   }
+  if (huge_size(nfft)) {
+    spx_status st = build_huge_plan(ctx, nfft, plan.get());
+    if (st != SPX_OK) return st;
+    *out = plan.get();
+    ctx->plans.emplace(key, std::move(plan));
+    return SPX_OK;
+  }
   if (!build_geom(nfft, &plan->g, ept, pref)) {
     if (!bluestein_size(nfft))
       return fail(ctx, SPX_ERR_INVALID_ARG,
                   "nfft=" + std::to_string(nfft) +
-                      " is not a supported size (2 .. 2^20 points, 2^a*3^b up to 262144, 2^21)");
+                      " is not a supported size (any length 2 .. 2^27; 2^a*3^b up to 2^28 with a split into"
+                      " two factors <= 16384)");
     spx_status st = build_bluestein_plan(ctx, nfft, plan.get());
     if (st != SPX_OK) return st;
     *out = plan.get();
@@ -423,6 +431,7 @@ spx_status launch_fft_out(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   if (beams == 0) return SPX_OK;
   if (plan.big) return launch_fft_big(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
   if (plan.bluestein) return launch_fft_bluestein(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
+  if (plan.huge) return launch_fft_huge(ctx, plan, d_in, beams, n_point, d_win, out_mode, scale, d_out);
   FftGeom g = plan.g;
   const float2* twl = plan.d_tw_local;
   const float2* twc = plan.d_tw_cross;

@@ -232,7 +232,7 @@ uint32_t spx_next_smooth23(uint32_t n) {
 
 int spx_fft_size_supported(uint32_t nfft) {
   FftGeom g;
-  return (build_geom(nfft, &g) || big_size(nfft) || bluestein_size(nfft)) ? 1 : 0;
+  return (build_geom(nfft, &g) || big_size(nfft) || huge_size(nfft) || bluestein_size(nfft)) ? 1 : 0;
 }
 
 spx_status spx_set_fft_tuning(spx_ctx* ctx, uint32_t nfft, uint32_t points_per_thread,
@@ -458,7 +458,7 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
       cap = params->max_per_beam;
     }
     const bool thr = params->thresh_sigma > 0.0f;
-    if (!plan->big && !plan->bluestein && fused_supported(plan->g, params->mode)) {
+    if (!plan->big && !plan->bluestein && !plan->huge && fused_supported(plan->g, params->mode)) {
       const float* win = nullptr;
       st = get_window(ctx, window, n_point, &win);
       if (st != SPX_OK) return st;

@@ -28,6 +28,12 @@ struct FftPlan {
   const FftPlan* sub = nullptr;  // the bm-point plan (owned by the context)
   float2* d_chirp = nullptr;     // w[n] = exp(-i pi n^2 / nfft), n < nfft
   float2* d_bfft = nullptr;      // FFT_bm of the conjugate chirp, wrapped
+  // Transforms of more than 2^21 points (fft_huge.cu): nfft = hn1 x hn2,
+  // sub = the hn1-point plan, sub2 = the hn2-point plan, d_tw_cross = the
+  // twiddle tables W_N^l (l < 2^hlshift), then W_N^{j 2^hlshift}.
+  bool huge = false;
+  uint32_t hn1 = 0, hn2 = 0, hlshift = 0;
+  const FftPlan* sub2 = nullptr;
   ~FftPlan();
 };
 
@@ -49,8 +55,8 @@ struct spx_ctx {
   std::map<uint32_t, std::pair<uint32_t, uint32_t>> tuning;  // nfft -> (points/thread, points/CTA)
   std::map<uint64_t, float*> windows;  // (window << 32 | n_point) -> table
   // Grow-on-demand device scratch, one buffer per slot (see spx::Slot).
-  void* d_scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  size_t scratch_bytes[5] = {0, 0, 0, 0, 0};
+  void* d_scratch[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t scratch_bytes[6] = {0, 0, 0, 0, 0, 0};
   uint32_t* d_error = nullptr;         // device error word (kErr* bits)
   uint32_t epoch = 0;                  // lookback status epoch
   // Host-buffer pipeline (spx_fft_peaks_host): copy streams, staging, events.
@@ -78,9 +84,10 @@ enum Slot : int {
   kSlotThresh = 1,  // per-beam noise thresholds
   kSlotSpectrum = 2, // intermediate spectra of composed (non-fused) calls
   kSlotExchange = 3, // per-cluster exchange slots of the large-FFT kernels
-  kSlotChirp = 4     // the padded chirp-z sequences of Bluestein transforms
+  kSlotChirp = 4,    // the padded chirp-z sequences of Bluestein transforms
+  kSlotHuge = 5      // the two transposed copies of a transform of more than 2^21 points
 };
-constexpr int kSlots = 5;
+constexpr int kSlots = 6;
 // Ensures at least `bytes` in `slot`; returns its device pointer.  Growing a
 // slot frees the old buffer (cudaFree waits for the device first).
 spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
@@ -89,8 +96,11 @@ spx_status get_scratch(spx_ctx* ctx, int slot, size_t bytes, void** out);
 // up to 16) once per (device, kernel).
 cudaError_t configure_kernel(const void* kernel, size_t max_smem);
 
-// Largest transform without a direct plan (Bluestein, through 2^21 points).
-constexpr uint32_t kMaxBluestein = 1u << 20;
+// Largest transform without a direct plan (Bluestein, through a power of
+// two of at most 2^28 points).
+constexpr uint32_t kMaxBluestein = 1u << 27;
+// Largest transform of the four-step path of fft_huge.cu (16384 x 16384).
+constexpr uint32_t kMaxHuge = 1u << 28;
 bool bluestein_size(uint32_t nfft);
 spx_status build_bluestein_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
 spx_status launch_fft_bluestein(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
@@ -102,6 +112,13 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
 spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
                           uint32_t n_point, const float* d_win, uint32_t out_mode, float scale,
                           void* d_out);
+
+// Transforms of more than 2^21 points: N1 x N2, both 2^a 3^b <= 16384 (fft_huge.cu).
+bool huge_size(uint32_t nfft);
+spx_status build_huge_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan);
+spx_status launch_fft_huge(spx_ctx* ctx, const FftPlan& plan, const float2* d_in, uint32_t beams,
+                           uint32_t n_point, const float* d_win, uint32_t out_mode, float scale,
+                           void* d_out);
 
 // Fused FFT + peak search (fft_peaks.cu).
 bool fused_supported(const FftGeom& g, uint32_t mode);

@@ -188,9 +188,23 @@ static void fft_tests(CudaBackend& be) {
     expect_throw<std::invalid_argument>("fft.size_mismatch",
                                         [&] { fft.ProcessComplex(std::vector<std::complex<float>>(199), p); });
     p.n_point = 1 << 20;
-    p.repeat_count = 4;  // 2^22: beyond this build's sizes
+    p.repeat_count = 512;  // 2^29: beyond this build's sizes
     expect_throw<std::invalid_argument>("fft.unsupported_nfft",
                                         [&] { fft.ProcessComplex(std::vector<std::complex<float>>(2 << 20), p); });
+  }
+  {  // nextPow2(2^20) x repeat_count 4 = 2^22 (the four-step transform): a tone at 1000 Hz of fs 2^20 Hz
+    FFTProcessorROCm fft(&be);
+    FFTProcessorParams p;
+    p.beam_count = 1;
+    p.n_point = 1 << 20;
+    p.sample_rate = (float)(1 << 20);
+    p.repeat_count = 4;
+    p.output_mode = FFTOutputMode::MAGNITUDE_PHASE;
+    auto r = fft.ProcessMagPhase(tone(1000.f, (float)(1 << 20), 1 << 20, 1), p);
+    const uint32_t n = r[0].nFFT;
+    const size_t pk = peak_bin(r[0].magnitude, n / 2);
+    check(n == (1u << 22) && pk == 4000 && std::fabs(r[0].magnitude[pk] - (float)(1 << 20)) < 10.0f,
+          "fft.repeat_count_four_step", "nFFT " + std::to_string(n) + " peak " + std::to_string(pk));
   }
 }
 
@@ -417,7 +431,7 @@ static void gpufft_tests() {
     check(Y.size() == n1 && e1 / p1 < 1e-5, "gpufft.any_length_1000", std::to_string(e1 / p1));
   }
   expect_throw<std::invalid_argument>("gpufft.unsupported_length", [] {
-    GpuFFT::ForwardC2C(std::vector<std::complex<float>>((1u << 20) + 1));
+    GpuFFT::ForwardC2C(std::vector<std::complex<float>>((1u << 27) + 1));  // too long for Bluestein's transform
   });
 }
 

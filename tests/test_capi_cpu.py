@@ -53,11 +53,17 @@ def test_next_smooth23_matches_oracle(lib):
 
 def test_fft_size_support(lib):
     """2^a 3^b sizes by the Stockham plans, 2^19 .. 2^21 by the three-launch
-    transform, every other length from 2 to 2^20 by Bluestein's transform."""
+    transform, 2^a 3^b sizes above 2^21 up to 2^28 that split into two
+    factors <= 16384 by the four-step transform, every other length from 2
+    to 2^27 by Bluestein's transform."""
     for n in (2, 3, 5, 7, 8, 1000, 1009, 4096, 13122, 59049, 104976, 131072, 262144, 524289, 3 << 18,
-              1 << 19, (1 << 20) - 1, 1 << 20, 1 << 21):
+              1 << 19, (1 << 20) - 1, 1 << 20, (1 << 20) + 1, 1 << 21, 3 << 20, 1 << 22, 3 << 21, 1 << 24,
+              3 ** 14, 3 ** 17, 1 << 27, (1 << 27) - 1, 1 << 28, (1 << 14) * 3 ** 8):
         assert lib.spx_fft_size_supported(n) == 1, n
-    for n in (0, 1, (1 << 20) + 1, 3 << 20, 1 << 22):
+    # too long for Bluestein's transform (non-smooth, > 2^27), beyond 2^28,
+    # or 3-smooth beyond 2^28 (3^18); 3^17 has no split into two factors
+    # <= 16384 and runs Bluestein's transform
+    for n in (0, 1, (1 << 27) + 1, (1 << 28) + 1, 1 << 29, 3 ** 18, 0xFFFFFFFF):
         assert lib.spx_fft_size_supported(n) == 0, n
 
 

@@ -111,12 +111,12 @@ def test_batch_autotune_keeps_results_and_plan_cache_round_trips(spx, cuda, tmp_
         b.tune(32)                      # batches run 16 points per thread
 
 
-@pytest.mark.parametrize("n_point,nfft", [(500000, 0), (4096, 1 << 20)])
+@pytest.mark.parametrize("n_point,nfft", [(500000, 0), (4096, 1 << 20), (4096, 1 << 22)])
 def test_batch_rejects_three_launch_sizes(spx, cuda, n_point, nfft):
-    """A beam whose transform is 2^19 or 2^20 points (the next 3-smooth size
-    of 500000 is 2^19, or an explicit nfft) is not a cluster of the batch
-    kernel: creation fails with SPX_ERR_UNSUPPORTED, nothing is launched, and
-    the context keeps working."""
+    """A beam whose transform is 2^19 points or more (the next 3-smooth size
+    of 500000 is 2^19, or an explicit nfft of 2^20 or of 2^22, a four-step
+    transform) is not a cluster of the batch kernel: creation fails with
+    SPX_ERR_UNSUPPORTED, nothing is launched, and the context keeps working."""
     from spectrum_gb300 import _capi
     from spectrum_gb300.batch import Batch
     n_points = [1000, n_point]
@@ -124,7 +124,7 @@ def test_batch_rejects_three_launch_sizes(spx, cuda, n_point, nfft):
     with pytest.raises(_capi.SpxError) as ei:
         Batch(n_points, nffts=nffts, window=spx.WINDOW_HANN, k=4, sample_rate=1.0)
     assert ei.value.status == _capi.SPX_ERR_UNSUPPORTED
-    assert "2^19 and 2^20" in str(ei.value)
+    assert "2^19 points and more" in str(ei.value)
     lengths, flat = _uneven(6, 1000, 5000, seed=11)
     b = Batch(lengths, window=spx.WINDOW_HANN, k=4, sample_rate=1.0)
     import torch

@@ -24,6 +24,9 @@ FFT_CASES = [
     (65536, 65536, 3), (69984, 69000, 1), (104976, 100000, 1), (131072, 65536, 1),
     (59049, 59049, 0), (262144, 262144, 0), (1 << 19, 300000, 1), (1 << 20, 1 << 20, 4),
     (1 << 21, 1 << 20, 1),  # nextPow2(2^20) x repeat_count 2, the reference's largest common FFTProcessor size
+    (1 << 22, 1 << 20, 1),  # nextPow2(2^20) x repeat_count 4: the four-step transform (2048 x 2048)
+    (3 << 21, 5000000, 4),  # 3-smooth above 2^21 (1536 x 4096), Blackman-Harris
+    (1 << 23, 1 << 23, 0),  # 2048 x 4096, no padding
 ]
 
 
@@ -41,7 +44,7 @@ def _max_rel(a, b):
 @pytest.mark.parametrize("nfft,n_point,win", FFT_CASES)
 def test_fft_complex_matches_pocketfft(spx, cuda, nfft, n_point, win):
     import torch
-    beams = 3 if nfft <= 65536 else (2 if nfft <= 262144 else 1)
+    beams = 3 if nfft <= 65536 else (2 if nfft <= 262144 or nfft >= (1 << 22) else 1)
     x = _signal(beams, n_point, nfft + n_point)
     got = spx.fft(torch.from_numpy(x).to(cuda), nfft, window=win).cpu().numpy()
     ref32 = orc.fft_fp32(x, nfft, win)
@@ -97,9 +100,11 @@ def test_fft_rejects_bad_sizes(spx, cuda):
     with pytest.raises(ValueError):
         spx.fft(x, 50)           # nfft < n_point
     with pytest.raises(ValueError):
-        spx.fft(x, (1 << 20) + 1)  # beyond 2^20 only 2^21 (no direct plan, too long for Bluestein)
+        spx.fft(x, (1 << 27) + 1)  # no direct plan, too long for Bluestein's transform
     with pytest.raises(ValueError):
-        spx.fft(x, 1 << 22)
+        spx.fft(x, 1 << 29)        # beyond the four-step transform's 2^28
+    with pytest.raises(ValueError):
+        spx.fft(x, 3 ** 18)        # 3-smooth beyond 2^28
 
 
 def test_precision_workload_dynamic_range(spx, cuda):
@@ -186,11 +191,14 @@ def test_fft_any_length_matches_reference_cpufft(spx, cuda, n):
 
 
 @pytest.mark.parametrize("nfft,n_point,win", [(5, 5, 0), (7, 6, 1), (1000, 900, 1), (1009, 1009, 4), (65537, 60000, 1),
-                                              ((1 << 20) - 1, 1 << 19, 2), (3 << 18, 700000, 0)])
+                                              ((1 << 20) - 1, 1 << 19, 2), (3 << 18, 700000, 0),
+                                              ((1 << 20) + 1, 1 << 20, 1), (5000011, 4000000, 1)])
 def test_bluestein_lengths_match_fp64(spx, cuda, nfft, n_point, win):
     """Lengths without a Stockham plan (primes, 5- and 7-smooth, 2^20 - 1,
-    3 2^18): every output mode against the FP64 transform of the windowed,
-    zero-padded samples, within 1e-5 of the peak; the inverse round-trips."""
+    3 2^18, 2^20 + 1 and the prime 5000011, whose power-of-two transforms of
+    2^22 and 2^24 points run the four-step path): every output mode against
+    the FP64 transform of the windowed, zero-padded samples, within 1e-5 of
+    the peak; the inverse round-trips."""
     import torch
     beams = 2 if nfft < (1 << 19) else 1
     x = _signal(beams, n_point, nfft)
@@ -228,7 +236,7 @@ def test_ifft_and_r2c_match_reference_cpufft(spx, cuda, n):
     np.testing.assert_array_equal(gf[:, : n // 2 + 1], gh)
 
 
-@pytest.mark.parametrize("nfft", [2, 9, 96, 4096, 13122, 65536, 131072, 1 << 20, 1 << 21])
+@pytest.mark.parametrize("nfft", [2, 9, 96, 4096, 13122, 65536, 131072, 1 << 20, 1 << 21, 1 << 22, 3 << 21])
 def test_ifft_round_trip_and_fp64(spx, cuda, nfft):
     import torch
     beams = 2 if nfft < (1 << 20) else 1
@@ -254,3 +262,27 @@ def test_r2c_window_and_padding(spx, cuda, n_point, nfft, win, full):
     got = spx.fft_r2c(torch.from_numpy(r).to(cuda), nfft, window=win, full=full).cpu().numpy()
     ref = orc.fft_r2c_fp32(r, nfft, win, full)
     assert np.abs(got - ref).max() / np.abs(ref).max() < FFT_TOL
+
+
+@pytest.mark.parametrize("nfft,n_point", [(1 << 22, 3000000), (1 << 24, 1 << 24)])
+def test_four_step_transform_modes_and_peaks(spx, cuda, nfft, n_point):
+    """Transforms above 2^21 points (the reference's nextPow2(n_point) x
+    repeat_count, fft_processor_rocm.cpp:673-677): |X| and |X|^2 epilogues
+    bit-exact against the formula on the complex output, the FP64 spectrum
+    within 1e-5 of the peak, and the top-K / all-maxima searches on the same
+    spectrum bit-exact against the oracle."""
+    import torch
+    x = _signal(1, n_point, nfft + 3)
+    xd = torch.from_numpy(x).to(cuda)
+    z = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    ref = orc.fft_fp64(x, nfft, orc.WINDOW_HANN)
+    assert _max_rel(z, ref) < FFT_TOL
+    mag = spx.fft(xd, nfft, window=spx.WINDOW_HANN, out="mag").cpu().numpy()
+    np.testing.assert_array_equal(mag, orc.magnitude(z))
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, spx.PEAK_TOPK, sample_rate=1.0, max_per_beam=8,
+                                refine=spx.REFINE_PARABOLIC)
+    got = spx.maxvalues_to_numpy(out)
+    want, wc = orc.topk(None, z, nfft, 1.0, 8)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), wc)
+    np.testing.assert_array_equal(got["index"], want["index"])
+    np.testing.assert_array_equal(got["refined_frequency"], want["refined_frequency"])
