@@ -94,8 +94,14 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, float2* __restri
   float2* row = scratch + (size_t)beam * g.nfft + (size_t)k1 * g.M;
   if (g.ahead && blockIdx.x + g.ahead < gridDim.x)  // the row the CTA one wave later reads
     prefetch_l2(row + (size_t)g.ahead * g.M, (size_t)g.M * sizeof(float2), tid, T);
-  local_fft<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tw_local, tid, T);
   // the row was read by this CTA alone (first pass, before its barrier)
+  if constexpr (EPT == 16) {
+    if (g.M == 16384 && T == 1024) {  // the last pass writes the row from its registers
+      ct_local_fft_out<16384>(s, SampleLoader{row, g.M, nullptr}, tw_local, tid, RowOutStream{row});
+      return;
+    }
+  }
+  local_fft<EPT>(s, g, SampleLoader{row, g.M, nullptr}, tw_local, tid, T);
   for (uint32_t i = tid; i < g.M; i += T) __stcs(row + i, s[sw(i)]);
 }
 

@@ -219,6 +219,18 @@ struct ExchangeLoader {
   SPX_DEV float2 operator()(uint32_t n) const { return __ldcg(row + n); }
 };
 
+// Output of a last local pass into a row of device memory: row[i] = Z[i]
+// (L2-kept stores for rows read again in the same launch or the next one,
+// streaming stores otherwise).
+struct RowOut {
+  float2* row;
+  SPX_DEV void operator()(uint32_t i, float2 z) const { __stcg(row + i, z); }
+};
+struct RowOutStream {
+  float2* row;
+  SPX_DEV void operator()(uint32_t i, float2 z) const { __stcs(row + i, z); }
+};
+
 // First Stockham pass (Ns = 1) reading its inputs from device memory.
 template <int R, int Q, typename Load>
 SPX_DEV void pass_first_global(float2* s, uint32_t M, const Load& load, uint32_t tid, uint32_t T) {
@@ -465,7 +477,9 @@ SPX_DEV void ct_first(float2* s, const Load& load, uint32_t tid) {
   __syncthreads();
 }
 
-// Pass P >= 1 in shared memory.
+// Pass P >= 1 in shared memory.  The last pass (Ns = M / R = B) writes each
+// butterfly's outputs to the elements it read (base = j), so it needs no
+// barrier between its loads and its stores.
 template <int M, int P, int T>
 SPX_DEV void ct_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
   using PL = CtPlan<M>;
@@ -480,7 +494,7 @@ SPX_DEV void ct_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
       for (int r = 0; r < R; ++r) v[q][r] = s[(B % 16 == 0) ? sj + sw(r * B) : sw(j + r * B)];
     }
   }
-  __syncthreads();
+  if constexpr (P + 1 < PL::npass) __syncthreads();
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const uint32_t j = tid + q * T;
@@ -512,12 +526,71 @@ SPX_DEV void ct_passes_from(float2* s, const float2* __restrict__ tw, uint32_t t
   }
 }
 
+// The last pass (P = npass - 1 >= 1) with its outputs handed to out(i, z)
+// (element i of the local FFT's natural-order result) instead of shared
+// memory: consecutive threads get consecutive i, so a store to a row in
+// device memory is coalesced.  Ends without a barrier.
+template <int M, int T, typename Out>
+SPX_DEV void ct_last_pass_out(const float2* s, const float2* __restrict__ tw, uint32_t tid, const Out& out) {
+  using PL = CtPlan<M>;
+  constexpr int P = PL::npass - 1;
+  constexpr int R = PL::radix(P), Ns = PL::ns(P), B = M / R, Q = (B + T - 1) / T;
+  static_assert(P >= 1 && Ns == B, "the last pass of the plan");
+  float2 v[Q][R];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
+      const uint32_t sj = sw(j);
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q][r] = s[(B % 16 == 0) ? sj + sw(r * B) : sw(j + r * B)];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint32_t j = tid + q * T;
+    if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
+      const float2* t = tw + PL::twoff(P) + j;  // k = j mod Ns = j
+      if constexpr (R == 4) {
+        const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
+        v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], __ldg(t + (r - 1) * Ns));
+      }
+      Dft<R>::run(v[q]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) out(j + r * B, v[q][r]);
+    }
+  }
+}
+
+template <int M, int P, int T>
+SPX_DEV void ct_passes_until_last(float2* s, const float2* __restrict__ tw, uint32_t tid) {
+  if constexpr (P + 1 < CtPlan<M>::npass) {
+    ct_pass<M, P, T>(s, tw, tid);
+    ct_passes_until_last<M, P + 1, T>(s, tw, tid);
+  }
+}
+
 // Whole local FFT of M points (first pass from `load`) by a CTA of T
 // threads, ending with a barrier.
 template <int M, int T = CtPlan<M>::T, typename Load>
 SPX_DEV void ct_local_fft(float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
   ct_first<M, T>(s, load, tid);
   ct_passes_from<M, 1, T>(s, tw, tid);
+}
+
+// The local FFT of ct_local_fft with the last pass's outputs handed to
+// out(i, z) (ct_last_pass_out) instead of shared memory; ends without a
+// barrier (the shared memory is still being read by the last pass).
+template <int M, int T = CtPlan<M>::T, typename Load, typename Out>
+SPX_DEV void ct_local_fft_out(float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid,
+                              const Out& out) {
+  static_assert(CtPlan<M>::npass >= 2, "at least one pass after the first");
+  ct_first<M, T>(s, load, tid);
+  ct_passes_until_last<M, 1, T>(s, tw, tid);
+  ct_last_pass_out<M, T>(s, tw, tid, out);
 }
 
 // The local sizes with an out-of-line compile-time plan (kernels that take

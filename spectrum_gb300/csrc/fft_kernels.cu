@@ -111,10 +111,10 @@ fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
     }
     group_barrier(arrive + beam, g.C, err);
     float2* row = slot + (size_t)c * M;
-    ct_local_fft<M>(s, ExchangeLoader{row}, tw_local, tid);
     // row c was read by this CTA alone: it takes the CTA's spectrum row
-    // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
-    for (uint32_t i = tid; i < M; i += T) __stcg(row + i, s[sw(i)]);
+    // (row[i] = X[c + C*i]) from the last pass's registers;
+    // rows_transpose_kernel writes the output
+    ct_local_fft_out<M>(s, ExchangeLoader{row}, tw_local, tid, RowOut{row});
   }  // (the next beam's group barrier orders these reads of s before its local FFT)
 }
 

@@ -262,19 +262,41 @@ SPX_DEV bool warp_median_window(const uint32_t* h, uint32_t W, uint32_t b0, uint
 // local FFT) takes this CTA's bins k = c + C*i in [start - 1, end + 1) (the
 // search window and the neighbours of its end bins): row[i] = X[c + C*i].
 // The rest of the row is discarded from L2.
-SPX_DEV void write_window_row(float2* row, const float2* s, const FftGeom& g, uint32_t c, uint32_t start,
-                              uint32_t end, uint32_t tid, uint32_t T) {
+struct WindowRows {
+  uint32_t ilo, ihi;  // row indices i of the CTA's window bins: [ilo, ihi)
+};
+SPX_DEV WindowRows window_rows(const FftGeom& g, uint32_t c, uint32_t start, uint32_t end) {
   const uint32_t klo = start - 1, khi = min(end + 1, g.nfft);
   const uint32_t ilo = klo <= c ? 0u : (klo - c + g.C - 1) / g.C;
   const uint32_t ihi = khi <= c ? 0u : min(g.M, (khi - c + g.C - 1) / g.C);
-  for (uint32_t i = ilo + tid; i < ihi; i += T) __stcg(row + i, s[sw(i)]);
-  if (ihi > ilo) {
-    discard_row_l2(row, (size_t)ilo * sizeof(float2), tid, T);
-    discard_row_l2(row + ihi, (size_t)(g.M - ihi) * sizeof(float2), tid, T);
+  return WindowRows{ilo, ihi};
+}
+
+// Drops from L2, without write-back, the lines of the row outside the window.
+SPX_DEV void discard_outside_window(float2* row, const FftGeom& g, WindowRows w, uint32_t tid, uint32_t T) {
+  if (w.ihi > w.ilo) {
+    discard_row_l2(row, (size_t)w.ilo * sizeof(float2), tid, T);
+    discard_row_l2(row + w.ihi, (size_t)(g.M - w.ihi) * sizeof(float2), tid, T);
   } else {
     discard_row_l2(row, (size_t)g.M * sizeof(float2), tid, T);
   }
 }
+
+SPX_DEV void write_window_row(float2* row, const float2* s, const FftGeom& g, uint32_t c, uint32_t start,
+                              uint32_t end, uint32_t tid, uint32_t T) {
+  const WindowRows w = window_rows(g, c, start, end);
+  for (uint32_t i = w.ilo + tid; i < w.ihi; i += T) __stcg(row + i, s[sw(i)]);
+  discard_outside_window(row, g, w, tid, T);
+}
+
+// Output of the last local pass straight into the window part of the row.
+struct WindowRowOut {
+  float2* row;
+  WindowRows w;
+  SPX_DEV void operator()(uint32_t i, float2 z) const {
+    if (i >= w.ilo && i < w.ihi) __stcg(row + i, z);
+  }
+};
 
 template <int EPT>
 __global__ void __launch_bounds__(kMaxLocal / EPT, 1)
@@ -352,9 +374,12 @@ fft_group_kernel(FftGeom g, FusedArgs a, uint32_t groups) {
     if (beam + groups < g.beams) cross(beam + groups);
     group_wait(a.arrive + beam, g.C, a.err);
     float2* row = a.xch + (size_t)beam * g.nfft + (size_t)c * M;
-    ct_local_fft<M>(s, ExchangeLoader{row}, a.tw_local, tid);
-    write_window_row(row, s, g, c, a.start, a.end, tid, T);
-  }
+    // the last pass writes the window's bins of the row straight from its
+    // registers (no store to shared memory, barrier and reload)
+    const WindowRows w = window_rows(g, c, a.start, a.end);
+    ct_local_fft_out<M>(s, ExchangeLoader{row}, a.tw_local, tid, WindowRowOut{row, w});
+    discard_outside_window(row, g, w, tid, T);
+  }  // (the next beam's group_arrive barrier orders these reads of s before its first pass)
 }
 
 // Self-test of the bounded wait: a single CTA arrives at a barrier that
