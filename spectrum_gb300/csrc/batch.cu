@@ -318,10 +318,12 @@ __global__ void __launch_bounds__(kBpThreads, 1) fft_batch_kernel(BatchArgs a) {
   const BatchBeam* bm = a.beams + d.beam;
   const BatchGeom* bg = a.geoms + bm->geom;
   float2* row = a.xch + bm->spec_off + (size_t)d.c * bg->g.M;
-  if (bg->g.ept != 16 || !ct_menu_fft<(int)kBpThreads>(bg->g.M, s, ExchangeLoader{row}, bg->twl, threadIdx.x))
-    bp_local_runtime(s, &bg->g, row, bg->twl);
   // row c was read by this CTA alone: it takes the CTA's spectrum row
-  for (uint32_t i = threadIdx.x; i < bg->g.M; i += kBpThreads) __stcg(row + i, s[sw(i)]);
+  if (bg->g.ept != 16 ||
+      !ct_menu_fft<(int)kBpThreads>(bg->g.M, s, ExchangeLoader{row}, bg->twl, threadIdx.x, RowOut{row})) {
+    bp_local_runtime(s, &bg->g, row, bg->twl);
+    for (uint32_t i = threadIdx.x; i < bg->g.M; i += kBpThreads) __stcg(row + i, s[sw(i)]);
+  }
 }
 
 }  // namespace spx

@@ -597,31 +597,33 @@ SPX_DEV void ct_local_fft_out(float2* s, const Load& load, const float2* __restr
 // many sizes call them through ct_menu_fft; one register allocation each).
 // Together they cover every 2^a 3^b transform of 16385 .. 262144 points as
 // C x M with C in {2, 3, 4, 6, 8, 9, 12, 16}, each at the largest such M.
-template <int M, int T, typename Load>
-__device__ __noinline__ void ct_local_fft_ool(float2* s, Load load, const float2* __restrict__ tw, uint32_t tid) {
-  ct_local_fft<M, T>(s, load, tw, tid);
+template <int M, int T, typename Load, typename Out>
+__device__ __noinline__ void ct_local_fft_ool(float2* s, Load load, const float2* __restrict__ tw, uint32_t tid,
+                                              Out out) {
+  ct_local_fft_out<M, T>(s, load, tw, tid, out);
 }
 
-// The compile-time local FFT of M points when M is in the menu (returns
-// true), else nothing (returns false).  The CTA has T threads, or the plan's
-// default count when T = 0.
-template <int T, typename Load>
-SPX_DEV bool ct_menu_fft(uint32_t M, float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid) {
+// The compile-time local FFT of M points, its last pass's outputs handed to
+// out(i, z), when M is in the menu (returns true), else nothing (returns
+// false).  The CTA has T threads, or the plan's default count when T = 0.
+template <int T, typename Load, typename Out>
+SPX_DEV bool ct_menu_fft(uint32_t M, float2* s, const Load& load, const float2* __restrict__ tw, uint32_t tid,
+                         const Out& out) {
   switch (M) {
-    case 4096: ct_local_fft_ool<4096, T ? T : CtPlan<4096>::T>(s, load, tw, tid); return true;
-    case 5832: ct_local_fft_ool<5832, T ? T : CtPlan<5832>::T>(s, load, tw, tid); return true;
-    case 6144: ct_local_fft_ool<6144, T ? T : CtPlan<6144>::T>(s, load, tw, tid); return true;
-    case 6561: ct_local_fft_ool<6561, T ? T : CtPlan<6561>::T>(s, load, tw, tid); return true;
-    case 8192: ct_local_fft_ool<8192, T ? T : CtPlan<8192>::T>(s, load, tw, tid); return true;
-    case 8748: ct_local_fft_ool<8748, T ? T : CtPlan<8748>::T>(s, load, tw, tid); return true;
-    case 9216: ct_local_fft_ool<9216, T ? T : CtPlan<9216>::T>(s, load, tw, tid); return true;
-    case 10368: ct_local_fft_ool<10368, T ? T : CtPlan<10368>::T>(s, load, tw, tid); return true;
-    case 11664: ct_local_fft_ool<11664, T ? T : CtPlan<11664>::T>(s, load, tw, tid); return true;
-    case 12288: ct_local_fft_ool<12288, T ? T : CtPlan<12288>::T>(s, load, tw, tid); return true;
-    case 13122: ct_local_fft_ool<13122, T ? T : CtPlan<13122>::T>(s, load, tw, tid); return true;
-    case 13824: ct_local_fft_ool<13824, T ? T : CtPlan<13824>::T>(s, load, tw, tid); return true;
-    case 15552: ct_local_fft_ool<15552, T ? T : CtPlan<15552>::T>(s, load, tw, tid); return true;
-    case 16384: ct_local_fft_ool<16384, T ? T : CtPlan<16384>::T>(s, load, tw, tid); return true;
+    case 4096: ct_local_fft_ool<4096, T ? T : CtPlan<4096>::T>(s, load, tw, tid, out); return true;
+    case 5832: ct_local_fft_ool<5832, T ? T : CtPlan<5832>::T>(s, load, tw, tid, out); return true;
+    case 6144: ct_local_fft_ool<6144, T ? T : CtPlan<6144>::T>(s, load, tw, tid, out); return true;
+    case 6561: ct_local_fft_ool<6561, T ? T : CtPlan<6561>::T>(s, load, tw, tid, out); return true;
+    case 8192: ct_local_fft_ool<8192, T ? T : CtPlan<8192>::T>(s, load, tw, tid, out); return true;
+    case 8748: ct_local_fft_ool<8748, T ? T : CtPlan<8748>::T>(s, load, tw, tid, out); return true;
+    case 9216: ct_local_fft_ool<9216, T ? T : CtPlan<9216>::T>(s, load, tw, tid, out); return true;
+    case 10368: ct_local_fft_ool<10368, T ? T : CtPlan<10368>::T>(s, load, tw, tid, out); return true;
+    case 11664: ct_local_fft_ool<11664, T ? T : CtPlan<11664>::T>(s, load, tw, tid, out); return true;
+    case 12288: ct_local_fft_ool<12288, T ? T : CtPlan<12288>::T>(s, load, tw, tid, out); return true;
+    case 13122: ct_local_fft_ool<13122, T ? T : CtPlan<13122>::T>(s, load, tw, tid, out); return true;
+    case 13824: ct_local_fft_ool<13824, T ? T : CtPlan<13824>::T>(s, load, tw, tid, out); return true;
+    case 15552: ct_local_fft_ool<15552, T ? T : CtPlan<15552>::T>(s, load, tw, tid, out); return true;
+    case 16384: ct_local_fft_ool<16384, T ? T : CtPlan<16384>::T>(s, load, tw, tid, out); return true;
     default: return false;
   }
 }
@@ -639,6 +641,22 @@ SPX_DEV void local_fft(float2* s, const FftGeom& g, const Load& load, const floa
   }
   first_pass_dispatch<EPT>(s, g, load, tid, T);
   local_passes<EPT>(s, g, 1, tw, tid, T);
+}
+
+// local_fft with the natural-order result handed to out(i, z), i < M: from
+// the last pass's registers for the compile-time plans, else read back from
+// shared memory after the last pass.  Ends without a barrier.
+template <int EPT, typename Load, typename Out>
+SPX_DEV void local_fft_out(float2* s, const FftGeom& g, const Load& load, const float2* __restrict__ tw,
+                           uint32_t tid, uint32_t T, const Out& out) {
+  if constexpr (EPT == 16) {
+    if (g.M == 16384 && T == 1024) return ct_local_fft_out<16384>(s, load, tw, tid, out);
+    if (g.M == 8192 && T == 512) return ct_local_fft_out<8192>(s, load, tw, tid, out);
+    if (g.M == 4096 && T == 256) return ct_local_fft_out<4096>(s, load, tw, tid, out);
+  }
+  first_pass_dispatch<EPT>(s, g, load, tid, T);
+  local_passes<EPT>(s, g, 1, tw, tid, T);
+  for (uint32_t i = tid; i < g.M; i += T) out(i, s[sw(i)]);
 }
 
 // Output modes of the inverse and real-input transforms (beyond spx_fft_out).
@@ -676,66 +694,15 @@ SPX_DEV void store_bin(void* __restrict__ out, uint32_t out_mode, float scale, c
   }
 }
 
-// Output epilogue: shared memory holds Z[i] = X[c + C*i] of one beam.
-SPX_DEV void epilogue_out(const float2* s, const FftGeom& g, uint32_t c, uint32_t beam,
-                          void* __restrict__ out, uint32_t out_mode, float scale, uint32_t tid,
-                          uint32_t T) {
-  const size_t obase = (size_t)beam * g.nfft + c;
-  switch (out_mode) {
-    case SPX_OUT_COMPLEX: {
-      float2* o = reinterpret_cast<float2*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = s[sw(i)];
-      break;
-    }
-    case SPX_OUT_MAG: {
-      float* o = reinterpret_cast<float*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag_rn(s[sw(i)]), scale);
-      break;
-    }
-    case SPX_OUT_MAG2: {
-      float* o = reinterpret_cast<float*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) o[(size_t)g.C * i] = __fmul_rn(mag2_rn(s[sw(i)]), scale);
-      break;
-    }
-    case SPX_OUT_MAGPHASE: {
-      float2* o = reinterpret_cast<float2*>(out) + obase;
-      for (uint32_t i = tid; i < g.M; i += T) {
-        float2 z = s[sw(i)];
-        o[(size_t)g.C * i] = make_float2(mag_rn(z), atan2f(z.y, z.x));
-      }
-      break;
-    }
-    case kOutComplexReversed: {  // IFFT(X)[n] = FFT(X)[(N - n) mod N] / N
-      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * g.nfft;
-      for (uint32_t i = tid; i < g.M; i += T) {
-        const uint32_t k = c + g.C * i, n = k == 0 ? 0u : g.nfft - k;
-        const float2 z = s[sw(i)];
-        o[n] = make_float2(__fmul_rn(z.x, scale), __fmul_rn(z.y, scale));
-      }
-      break;
-    }
-    case kOutR2CHalf: {
-      const uint32_t half = g.nfft / 2;
-      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * (half + 1);
-      for (uint32_t i = tid; i < g.M; i += T) {
-        const uint32_t k = c + g.C * i;
-        if (k <= half) o[k] = s[sw(i)];
-      }
-      break;
-    }
-    default: {  // kOutR2CFull: the half spectrum and its conjugate mirror
-      const uint32_t half = g.nfft / 2;
-      float2* o = reinterpret_cast<float2*>(out) + (size_t)beam * g.nfft;
-      for (uint32_t i = tid; i < g.M; i += T) {
-        const uint32_t k = c + g.C * i;
-        if (k > half) continue;
-        const float2 z = s[sw(i)];
-        o[k] = z;
-        if (k >= 1 && k < g.nfft - half) o[g.nfft - k] = make_float2(z.x, -z.y);
-      }
-      break;
-    }
-  }
-}
+// Output of bin k = i of one beam's natural-order spectrum (C = 1) in any
+// output mode (the layouts of store_bin), for local_fft_out.
+struct BinOut {
+  void* out;
+  uint32_t out_mode;
+  float scale;
+  const FftGeom* g;
+  uint32_t beam;
+  SPX_DEV void operator()(uint32_t i, float2 z) const { store_bin(out, out_mode, scale, *g, beam, i, z); }
+};
 
 }  // namespace spx

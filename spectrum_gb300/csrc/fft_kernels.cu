@@ -33,8 +33,9 @@ fft_out_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __r
   const uint32_t tid = threadIdx.x, T = blockDim.x;
   const uint32_t beam = blockIdx.x;
   prefetch_future_beam(g, in, n_point, beam, 0, tid, T);
-  local_fft<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tw_local, tid, T);
-  epilogue_out(s, g, 0, beam, out, out_mode, scale, tid, T);
+  // C = 1: bin k is element k of the local result, written by the last pass
+  local_fft_out<EPT>(s, g, SampleLoader{in + (size_t)beam * n_point, n_point, win}, tw_local, tid, T,
+                     BinOut{out, out_mode, scale, &g, beam});
 }
 
 // ---------------------------------------------------------------------------
@@ -72,11 +73,10 @@ fft_xl_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __re
   }
   cl.sync();
   float2* row = slot + (size_t)c * g.M;
-  if (EPT != 16 || !ct_menu_fft<0>(g.M, s, ExchangeLoader{row}, tw_local, tid))
-    local_fft<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T);
   // row c was read by this CTA alone: it takes the CTA's spectrum row
   // (row[i] = X[c + C*i]); rows_transpose_kernel writes the output
-  for (uint32_t i = tid; i < g.M; i += T) __stcg(row + i, s[sw(i)]);
+  if (EPT != 16 || !ct_menu_fft<0>(g.M, s, ExchangeLoader{row}, tw_local, tid, RowOut{row}))
+    local_fft_out<EPT>(s, g, ExchangeLoader{row}, tw_local, tid, T, RowOut{row});
 }
 
 // The same transform as fft_xl_kernel for power-of-two local sizes M (M / 16
