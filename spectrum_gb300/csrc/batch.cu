@@ -163,12 +163,6 @@ __device__ __noinline__ void bp_local_runtime(float2* s, const FftGeom* g, const
 }
 
 // ---- top-K --------------------------------------------------------------------
-SPX_DEV uint64_t bt_insert(uint64_t mine, uint64_t x, uint32_t lane) {
-  const uint64_t up = __shfl_up_sync(0xffffffffu, mine, 1);
-  if (mine >= x) return mine;
-  return (lane == 0 || up >= x) ? x : up;
-}
-
 // Bins of a beam in row layout, written by the previous launch: bin q*CC + r
 // is element q of row r (rows M apart).
 struct RowBins {
@@ -219,7 +213,7 @@ SPX_DEV uint64_t bt_scan(const Bins& bins, uint32_t start, uint32_t end, uint32_
       while (want) {
         const int src = __ffs(want) - 1;
         want &= want - 1;
-        mine = bt_insert(mine, __shfl_sync(0xffffffffu, key, src), lane);
+        mine = warp_list_insert(mine, __shfl_sync(0xffffffffu, key, src), lane);
       }
     }
   }
@@ -262,15 +256,8 @@ topk_batch_kernel(const float2* __restrict__ xch, const BatchBeam* __restrict__ 
       default: mine = bt_scan<16, kBtThreads>(bins, start, end, a.K, lane, warp); break;
     }
   }
-  lists[warp][lane] = mine;
-  __syncthreads();
+  mine = merge_warp_lists(&lists[0][0], mine, kBtThreads / 32, a.K, warp, lane);
   if (warp != 0) return;
-  for (uint32_t w = 1; w < kBtThreads / 32; ++w)
-    for (uint32_t e = 0; e < a.K; ++e) {
-      const uint64_t x = lists[w][e];
-      if (x == 0) break;
-      mine = bt_insert(mine, x, lane);
-    }
   const uint32_t n = __popc(__ballot_sync(0xffffffffu, lane < a.K && mine != 0));
   if (lane == 0) a.counts[beam] = n;
   if (lane < n) {

@@ -157,17 +157,8 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
     }
     uint64_t* lists = reinterpret_cast<uint64_t*>(shist);  // histogram no longer needed
     __syncthreads();
-    lists[warp * 32 + lane] = mine;
-    __syncthreads();
+    mine = merge_warp_lists(lists, mine, nw, a.K, warp, lane);
     if (warp != 0) return;
-    for (uint32_t w = 1; w < nw; ++w) {
-      for (uint32_t e = 0; e < a.K; ++e) {
-        const uint64_t xk = lists[w * 32 + e];
-        if (xk == 0) break;
-        const uint64_t up = __shfl_up_sync(0xffffffffu, mine, 1);
-        if (mine < xk) mine = (lane == 0 || up >= xk) ? xk : up;
-      }
-    }
     const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, lane < a.K && mine != 0));
     if (lane == 0) a.counts[beam] = cnt;
     if (lane < cnt) {

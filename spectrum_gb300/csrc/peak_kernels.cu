@@ -502,13 +502,6 @@ SPX_DEV uint64_t topk_key(float mag, uint32_t bin) {
   return ((uint64_t)__float_as_uint(mag) << 32) | (uint32_t)(~bin);
 }
 
-// Insert x into the warp's descending list (lane l holds entry l).
-SPX_DEV uint64_t list_insert(uint64_t mine, uint64_t x, uint32_t lane) {
-  const uint64_t up = __shfl_up_sync(0xffffffffu, mine, 1);
-  if (mine >= x) return mine;
-  return (lane == 0 || up >= x) ? x : up;
-}
-
 SPX_DEV float mag_at(const float* mag, const float2* fft, size_t i) {
   return mag ? __ldg(mag + i) : mag_rn(__ldg(fft + i));
 }
@@ -566,20 +559,12 @@ topk_kernel(const float* __restrict__ mag, const float2* __restrict__ fft, uint3
         const int src = __ffs(want) - 1;
         want &= want - 1;
         const uint64_t x = __shfl_sync(0xffffffffu, key, src);
-        mine = list_insert(mine, x, lane);
+        mine = warp_list_insert(mine, x, lane);
       }
     }
   }
-  lists[warp][lane] = mine;
-  __syncthreads();
+  mine = merge_warp_lists(&lists[0][0], mine, kTkWarps, K, warp, lane);
   if (warp != 0) return;
-  for (uint32_t w = 1; w < kTkWarps; ++w) {
-    for (uint32_t e = 0; e < K; ++e) {
-      const uint64_t x = lists[w][e];
-      if (x == 0) break;
-      mine = list_insert(mine, x, lane);
-    }
-  }
   const uint32_t n = __popc(__ballot_sync(0xffffffffu, lane < K && mine != 0));
   if (lane == 0) counts[beam] = n;
   if (lane < n) {

@@ -458,7 +458,18 @@ spx_status spx_fft_peaks(spx_ctx* ctx, const void* d_in, uint32_t beams, uint32_
       cap = params->max_per_beam;
     }
     const bool thr = params->thresh_sigma > 0.0f;
-    if (!plan->big && !plan->bluestein && !plan->huge && fused_supported(plan->g, params->mode)) {
+    // nfft <= 16384 (one CTA per beam): the fused kernel keeps the spectrum
+    // on chip, but its search phase holds the SM from the next beam's
+    // transform, which pays only while the launch is short.  Measured on
+    // GB300 (8 .. 4096 beams of 4096 .. 16384 points, top-1/8 and 6-sigma
+    // all maxima), fused is faster for top-K at 4096 points or up to 2^23
+    // points in all, and for all maxima up to 2^21 points in all; beyond, the
+    // spectrum in device memory and a separate search kernel win (e.g. 4096
+    // x 16384 top-8: 0.597 vs 0.463 ms).  Both give the same bits.
+    const uint64_t pts = (uint64_t)beams * nfft;
+    const bool single_cta_pays =
+        plan->g.C > 1 || (all ? pts <= (1ull << 21) : (nfft <= 4096 || pts <= (1ull << 23)));
+    if (!plan->big && !plan->bluestein && !plan->huge && single_cta_pays && fused_supported(plan->g, params->mode)) {
       const float* win = nullptr;
       st = get_window(ctx, window, n_point, &win);
       if (st != SPX_OK) return st;

@@ -243,6 +243,38 @@ struct Dft<16> {
   }
 };
 
+// ---- top-K lists ------------------------------------------------------------
+// A warp's list: lane l holds entry l of its K largest keys (descending; 0 =
+// empty).  Inserting key x keeps the K largest.
+SPX_DEV uint64_t warp_list_insert(uint64_t mine, uint64_t x, uint32_t lane) {
+  const uint64_t up = __shfl_up_sync(0xffffffffu, mine, 1);
+  if (mine >= x) return mine;
+  return (lane == 0 || up >= x) ? x : up;
+}
+
+// Merges the lists of the CTA's nw warps into warp 0's, pairwise in
+// log2(nw) rounds (round s: warp w, a multiple of 2s, takes the list of warp
+// w + s): K log2(nw) insertions on the critical path instead of K (nw - 1).
+// The top K of a union does not depend on the order of the merges, so the
+// result is the serial merge's.  lists: nw x 32 words of shared memory, free
+// on entry; every thread of the CTA calls it; warp 0 gets the merged entry.
+SPX_DEV uint64_t merge_warp_lists(uint64_t* lists, uint64_t mine, uint32_t nw, uint32_t K, uint32_t warp,
+                                  uint32_t lane) {
+  lists[warp * 32 + lane] = mine;
+  for (uint32_t step = 1; step < nw; step *= 2) {
+    __syncthreads();
+    if (warp % (2 * step) == 0 && warp + step < nw) {
+      for (uint32_t e = 0; e < K; ++e) {
+        const uint64_t x = lists[(warp + step) * 32 + e];
+        if (x == 0) break;
+        mine = warp_list_insert(mine, x, lane);
+      }
+      lists[warp * 32 + lane] = mine;
+    }
+  }
+  return mine;
+}
+
 // ---- MaxValue (32 bytes, the reference's GPU layout) -------------------------
 struct MaxValueDev {
   uint32_t index;

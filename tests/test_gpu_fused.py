@@ -96,6 +96,27 @@ def test_fused_topk_single_cta(spx, cuda, nfft, k, sigma):
     assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
 
 
+@pytest.mark.parametrize("nfft,beams,mode,k,sigma", [(4096, 600, "all", 1000, 6.0), (8192, 1100, "topk", 8, 0.0),
+                                                     (16384, 600, "topk", 4, 3.0)])
+def test_fft_peaks_beyond_the_single_cta_limit(spx, cuda, nfft, beams, mode, k, sigma):
+    """spx_fft_peaks calls too large for the single-CTA fused kernel to pay
+    (the spectrum goes to device memory, then the search kernel): the same
+    counts and records as the oracle on spx_fft's spectrum."""
+    import torch
+    x = _beams(beams, nfft, nfft + beams, tones=(1, 4))
+    xd = torch.from_numpy(x).to(cuda)
+    spec = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    pm = spx.PEAK_ALL if mode == "all" else spx.PEAK_TOPK
+    out, counts = spx.fft_peaks(xd, nfft, spx.WINDOW_HANN, pm, sample_rate=1.0, max_per_beam=k, refine=1,
+                                thresh_sigma=sigma)
+    if mode == "all":
+        ref, rc = orc.all_maxima(None, spec, nfft, 1.0, 0, 0, k, refine=1, thresh_sigma=sigma)
+    else:
+        ref, rc = orc.topk(None, spec, nfft, 1.0, k, thresh_sigma=sigma)
+    np.testing.assert_array_equal(counts.cpu().numpy().astype(np.uint32), rc)
+    assert_rows_equal(spx.maxvalues_to_numpy(out), ref, rc)
+
+
 def test_fused_large_workload_properties(spx, cuda):
     """The benchmark workload's full size (256 x 65536 -> 131072): properties
     that need no full oracle run — every reported maximum exceeds its
