@@ -326,16 +326,24 @@ spx_status spx_fft_peaks_host(spx_ctx* ctx, const void* h_in, uint32_t beams,
  *  spx_batch_tune          every size at the largest local size <= points_per_cta
  *                          (points_per_thread must be 16)
  *  spx_batch_local_size / spx_batch_set_local_size  one size's plan
+ *  spx_batch_cluster / spx_batch_set_cluster  CTAs per cluster of the single
+ *                          launch: 0 = the largest C of the batch's beams, or
+ *                          any size from that to 16 (several beams share a
+ *                          cluster; how many clusters fit at once depends on
+ *                          how the size divides the GPU's SM groups)
  *  spx_batch_autotune      per distinct nfft, times the whole batch on the
  *                          given buffers with each candidate local size of that
  *                          nfft and keeps the fastest (the current plan unless
- *                          another is faster by over 2 %); *sizes_tuned = sizes
- *                          with more than one candidate, *sizes_changed = plans
- *                          changed
+ *                          another is faster by over 2 %), then each cluster
+ *                          size from the largest C to 16 the same way;
+ *                          *sizes_tuned = sizes with more than one candidate,
+ *                          *sizes_changed = plans changed (the cluster size
+ *                          counts as one)
  *  spx_batch_save_plans / spx_batch_load_plans  the plans as a JSON file
- *                          {"arch": "sm_XY", "plans": {"<nfft>": M, ...}};
- *                          loading applies the entries valid for the batch's
- *                          sizes on a device of that architecture */
+ *                          {"arch": "sm_XY", "plans": {"<nfft>": M, ...},
+ *                          "cluster": N}; loading applies the entries valid
+ *                          for the batch's sizes on a device of that
+ *                          architecture */
 typedef struct spx_batch spx_batch;
 spx_status spx_batch_create(spx_ctx* ctx, uint32_t beams, const uint32_t* n_points,
                             const uint32_t* nffts, uint32_t window,
@@ -352,6 +360,8 @@ spx_status spx_batch_replay(spx_ctx* ctx, spx_batch* batch);
 spx_status spx_batch_tune(spx_ctx* ctx, spx_batch* batch, uint32_t points_per_thread,
                           uint32_t points_per_cta);
 uint32_t spx_batch_local_size(const spx_batch* batch, uint32_t nfft);
+uint32_t spx_batch_cluster(const spx_batch* batch);
+spx_status spx_batch_set_cluster(spx_ctx* ctx, spx_batch* batch, uint32_t cluster);
 spx_status spx_batch_set_local_size(spx_ctx* ctx, spx_batch* batch, uint32_t nfft,
                                     uint32_t local_size);
 spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,

@@ -103,6 +103,8 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_batch_tune": (_i, [_vp, _vp, _u32, _u32]),
     "spx_batch_local_size": (_u32, [_vp, _u32]),
     "spx_batch_set_local_size": (_i, [_vp, _vp, _u32, _u32]),
+    "spx_batch_cluster": (_u32, [_vp]),
+    "spx_batch_set_cluster": (_i, [_vp, _vp, _u32]),
     "spx_batch_autotune": (_i, [_vp, _vp, _vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32)]),
     "spx_batch_save_plans": (_i, [_vp, _vp, C.c_char_p]),
     "spx_batch_load_plans": (_i, [_vp, _vp, C.c_char_p, C.POINTER(_u32)]),

@@ -96,6 +96,16 @@ class Batch:
         self.ctx.check(lib.spx_batch_set_local_size(self.ctx.h, self.h, int(nfft), int(local_size)))
 
     @property
+    def cluster(self) -> int:
+        """CTAs per cluster of the single FFT launch."""
+        return int(lib.spx_batch_cluster(self.h))
+
+    def set_cluster(self, cluster: int):
+        """CTAs per cluster of the single FFT launch (0: the largest C the
+        beams need; else that or more, up to 16)."""
+        self.ctx.check(lib.spx_batch_set_cluster(self.ctx.h, self.h, int(cluster)))
+
+    @property
     def plans(self) -> dict:
         """{nfft: local size} of the batch's distinct sizes."""
         return {int(n): self.local_size(int(n)) for n in sorted(set(self.nffts))}

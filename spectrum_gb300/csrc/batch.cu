@@ -6,7 +6,8 @@
 // a run.  A run is two launches:
 //   1. fft_batch_kernel: every beam's windowed, zero-padded FFT in ONE
 //      launch.  Beam b with nfft = C x M takes C CTAs (ranks 0..C-1) of one
-//      cluster; a cluster of Cl CTAs (Cl = the largest C) hosts one or
+//      cluster; a cluster of Cl CTAs (Cl = the largest C, or more, chosen
+//      by spx_batch_set_cluster or the autotuner) hosts one or
 //      several beams on disjoint rank ranges (first-fit decreasing, largest
 //      beams first).  A CTA runs the cross stage of its rank (C > 1: the
 //      C-point DFTs of its columns, window and zero padding on load, into the
@@ -335,6 +336,7 @@ struct spx_batch {
   float fs = 1.0f;
   std::vector<uint32_t> n_point, nfft;
   std::map<uint32_t, uint32_t> local;  // nfft -> local FFT size M of its plan (C = nfft / M)
+  uint32_t cluster_pref = 0;           // CTAs per cluster of the single launch (0: the largest C)
   uint64_t in_total = 0, spec_total = 0;
   LaunchSet all;                       // the single batched launch
   std::vector<LaunchSet> per_size;     // one launch per distinct nfft
@@ -424,6 +426,13 @@ std::vector<BatchCta> pack(std::vector<uint32_t> ids, const std::vector<uint32_t
   return ctas;
 }
 
+// The most CTAs any beam of the batch takes (C = nfft / M of its plan).
+uint32_t largest_c(const spx_batch* b) {
+  uint32_t c = 1;
+  for (const auto& kv : b->local) c = std::max(c, kv.first / kv.second);
+  return c;
+}
+
 // Tables and launch sets from the batch's plan choices.
 spx_status build(spx_ctx* ctx, spx_batch* b) {
   for (void* p : b->tables) cudaFree(p);
@@ -456,6 +465,10 @@ spx_status build(spx_ctx* ctx, spx_batch* b) {
   auto make_set = [&](const std::vector<uint32_t>& ids, uint32_t nfft, LaunchSet* ls) -> spx_status {
     uint32_t cl = 1;
     for (uint32_t id : ids) cl = std::max(cl, group[id]);
+    // the single launch may use larger clusters than its largest beam needs
+    // (several beams per cluster): how many fit at once depends on how the
+    // cluster size divides the GPU's SM groups
+    if (nfft == 0 && b->cluster_pref > cl) cl = b->cluster_pref;
     const std::vector<BatchCta> ctas = pack(ids, group, b->nfft, cl);
     ls->nfft = nfft;
     ls->n_ctas = (uint32_t)ctas.size();
@@ -783,6 +796,29 @@ spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,
     ++tuned;
     if (best_m != was) ++changed;
   }
+  // then the cluster size of the single launch: from the largest C to 16
+  if (st == SPX_OK) {
+    const uint32_t maxc = largest_c(batch);
+    const uint32_t was = batch->cluster_pref;
+    uint32_t best_cl = was;
+    float best = 1e30f, best_was = 1e30f;
+    for (uint32_t cl = maxc; cl <= kBtMaxC && st == SPX_OK; ++cl) {
+      batch->cluster_pref = cl == maxc ? 0u : cl;
+      if (resident_ctas((const void*)fft_batch_kernel, kBpThreads, kBpSmem, cl) == 0) continue;
+      st = build(ctx, batch);
+      float ms = 0.f;
+      if (st == SPX_OK) st = time_batch(&ms);
+      if (st != SPX_OK) break;
+      if (batch->cluster_pref == was) best_was = ms;
+      if (ms < best) {
+        best = ms;
+        best_cl = batch->cluster_pref;
+      }
+    }
+    if (best_cl != was && best_was < 1e30f && best > 0.98f * best_was) best_cl = was;
+    batch->cluster_pref = best_cl;
+    if (best_cl != was) ++changed;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   spx_status st2 = build(ctx, batch);
@@ -793,7 +829,7 @@ spx_status spx_batch_autotune(spx_ctx* ctx, spx_batch* batch, const void* d_in,
 }
 
 // Plan cache: one JSON object per file,
-//   {"arch": "sm_103", "plans": {"<nfft>": <local size>, ...}}
+//   {"arch": "sm_103", "plans": {"<nfft>": <local size>, ...}, "cluster": <CTAs per cluster, 0: the largest C>}
 spx_status spx_batch_save_plans(spx_ctx* ctx, const spx_batch* batch, const char* path) {
   if (!ctx || !batch) return SPX_ERR_INVALID_ARG;
   if (!path) return fail(ctx, SPX_ERR_INVALID_ARG, "spx_batch_save_plans: path is null");
@@ -807,7 +843,7 @@ spx_status spx_batch_save_plans(spx_ctx* ctx, const spx_batch* batch, const char
     f << (first ? "" : ", ") << "\"" << kv.first << "\": " << kv.second;
     first = false;
   }
-  f << "}}\n";
+  f << "}, \"cluster\": " << batch->cluster_pref << "}\n";
   f.close();
   return f ? SPX_OK : fail(ctx, SPX_ERR_INVALID_ARG, "spx_batch_save_plans: write failed");
 }
@@ -850,10 +886,35 @@ spx_status spx_batch_load_plans(spx_ctx* ctx, spx_batch* batch, const char* path
     const size_t comma = text.find(',', colon);
     p = comma == std::string::npos ? close : comma + 1;
   }
+  // "cluster": N (0 = the largest C); applied when valid for the batch
+  const size_t pc = text.find("\"cluster\"", close);
+  if (pc != std::string::npos) {
+    const size_t colon = text.find(':', pc);
+    const unsigned long cl = colon == std::string::npos ? 0ul : std::strtoul(text.c_str() + colon + 1, nullptr, 10);
+    if (cl <= kBtMaxC && (cl == 0 || cl >= largest_c(batch))) batch->cluster_pref = (uint32_t)cl;
+  }
   Guard gd(ctx->device);
   spx_status st = build(ctx, batch);
   if (applied) *applied = n_applied;
   return st;
+}
+
+uint32_t spx_batch_cluster(const spx_batch* batch) { return batch ? batch->all.cluster : 0u; }
+
+spx_status spx_batch_set_cluster(spx_ctx* ctx, spx_batch* batch, uint32_t cluster) {
+  if (!ctx || !batch) return SPX_ERR_INVALID_ARG;
+  if (cluster > kBtMaxC)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_batch_set_cluster: at most 16 CTAs per cluster");
+  const uint32_t need = largest_c(batch);
+  if (cluster != 0 && cluster < need)
+    return fail(ctx, SPX_ERR_INVALID_ARG, "spx_batch_set_cluster: a beam of the batch needs " +
+                                              std::to_string(need) + " CTAs per cluster");
+  Guard gd(ctx->device);
+  if (cluster != 0 && resident_ctas((const void*)fft_batch_kernel, kBpThreads, kBpSmem, cluster) == 0)
+    return fail(ctx, SPX_ERR_UNSUPPORTED, "spx_batch_set_cluster: no cluster of " + std::to_string(cluster) +
+                                              " CTAs fits the device");
+  batch->cluster_pref = cluster;
+  return build(ctx, batch);
 }
 
 }  // extern "C"

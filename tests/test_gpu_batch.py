@@ -92,21 +92,28 @@ def test_batch_autotune_keeps_results_and_plan_cache_round_trips(spx, cuda, tmp_
                              max_per_beam=4, refine=spx.REFINE_PARABOLIC, ctx=ctx)
         _same(spx.maxvalues_to_numpy(o)[0, :int(c[0])], g2[i, :int(c[0])])
         off += int(n)
-    # force a different plan for 93312 = 6 x 15552 = 8 x 11664 and round-trip the cache
+    # force a different plan for 93312 = 6 x 15552 = 8 x 11664 and a larger
+    # cluster than the largest C, and round-trip the cache
     b.set_local_size(93312, 11664)
     assert b.local_size(93312) == 11664
+    b.set_cluster(16)  # at least the largest C, whatever the autotuner chose
+    assert b.cluster == 16
     path = tmp_path / "plans.json"
     b.save_plans(path)
-    assert '"93312": 11664' in path.read_text()
+    assert '"93312": 11664' in path.read_text() and '"cluster": 16' in path.read_text()
     b2 = Batch(n_points, window=1, k=4, ctx=spx.Context(0))
     assert b2.load_plans(path) == len(b.plans)
-    assert b2.plans == b.plans
+    assert b2.plans == b.plans and b2.cluster == 16
     o3, c3 = [t.clone() for t in b.run(xd)]
     o4, c4 = [t.clone() for t in b2.run(xd)]
     np.testing.assert_array_equal(c3.cpu().numpy(), c4.cpu().numpy())
     _same(spx.maxvalues_to_numpy(o3), spx.maxvalues_to_numpy(o4))
     with pytest.raises(ValueError):
         b.set_local_size(93312, 1000)   # not C x M with C in the batch's cluster sizes
+    with pytest.raises(ValueError):
+        b.set_cluster(2)                # smaller than the >= 8 CTAs of 93312 = 8 x 11664
+    with pytest.raises(ValueError):
+        b.set_cluster(17)               # beyond 16
     with pytest.raises(spx._capi.SpxError):
         b.tune(32)                      # batches run 16 points per thread
 
@@ -130,3 +137,20 @@ def test_batch_rejects_three_launch_sizes(spx, cuda, n_point, nfft):
     import torch
     out, counts = b.run(torch.from_numpy(flat).to(cuda))
     assert int(counts.min()) >= 1
+
+
+@pytest.mark.parametrize("cluster", [0, 9, 10, 12, 16])
+def test_batch_cluster_size_keeps_results(spx, cuda, cluster):
+    """Any cluster size of the single launch from the largest C up to 16
+    packs the same beams differently and gives the same lists bit for bit."""
+    import torch
+    from spectrum_gb300.batch import Batch
+    n_points, x = _uneven(24, 1000, 60000, 29, extra=(59049, 80000))
+    xd = torch.from_numpy(x).to(cuda)
+    b = Batch(n_points, window=spx.WINDOW_HANN, k=8, sample_rate=1.0)
+    o1, c1 = [t.clone() for t in b.run(xd)]
+    b.set_cluster(cluster)
+    assert b.cluster == (9 if cluster == 0 else cluster)  # 59049 = 9 x 6561
+    o2, c2 = [t.clone() for t in b.run(xd)]
+    np.testing.assert_array_equal(c1.cpu().numpy(), c2.cpu().numpy())
+    _same(spx.maxvalues_to_numpy(o1), spx.maxvalues_to_numpy(o2))
