@@ -117,15 +117,7 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
   plan->g = gl;
   plan->big = true;
   std::vector<float2> twl(kBigM);
-  for (uint32_t p = 0; p < gl.npass; ++p) {
-    const uint32_t R = gl.radix[p], Ns = gl.ns[p];
-    for (uint32_t r = 1; r <= tw_rows(R); ++r)
-      for (uint32_t k = 0; k < Ns; ++k) {
-        const uint64_t L = (uint64_t)Ns * R, m = ((uint64_t)r * k) % L;
-        const double a = -2.0 * M_PI * (double)m / (double)L;
-        twl[gl.twoff[p] + (r - 1) * Ns + k] = make_float2((float)std::cos(a), (float)std::sin(a));
-      }
-  }
+  fill_local_twiddles(gl, twl.data());
   // [k1][n2] = W_N^{n2 k1} (n2 < kBigM, k1 < Cb, so n2 k1 < nfft: no reduction),
   // then the Cb entries W_Cb^e = W_N^{e kBigM}
   const uint32_t cb = gl.C;

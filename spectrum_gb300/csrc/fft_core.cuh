@@ -19,7 +19,8 @@
 // Shared memory layout: element i at sw(i) (spx_device.cuh), sw_len(M)
 // elements per local FFT.  Twiddles are FP32 values of FP64-generated
 // exponentials: tw_local holds, per pass p with radix R and stride Ns,
-// W_{Ns R}^{r k} at [(r-1)*Ns + k] for r <= tw_rows(R) (radix 4: r = 1 only);
+// W_{Ns R}^{r k} at [(r-1)*Ns + k] for r <= tw_rows(R) (radix 4: r = 1 only,
+// and for Ns >= kTwSplitNs two factor tables, tw_split in spx_geom.h);
 // tw_cross holds W_N^{n2} at [n2] (the cross stage forms W_N^{n2 k1} from it).
 #pragma once
 
@@ -165,6 +166,12 @@ SPX_DEV float2 load_sample(const float2* __restrict__ x, uint32_t n,
   return a;
 }
 
+// W_{4 Ns}^k of a radix-4 pass from its table t (tw_split layouts: two
+// factors for Ns >= kTwSplitNs).
+SPX_DEV float2 tw4(const float2* __restrict__ t, uint32_t k, uint32_t Ns) {
+  return Ns >= kTwSplitNs ? cmul(__ldg(t + 64 + (k >> 6)), __ldg(t + (k & 63u))) : __ldg(t + k);
+}
+
 // One in-place Stockham pass over shared memory.  Loads all of a thread's
 // butterflies, synchronises, computes, stores, synchronises.
 template <int R, int Q>
@@ -188,7 +195,7 @@ SPX_DEV void pass_smem(float2* s, uint32_t M, uint32_t Ns, uint32_t magic,
       const uint32_t k = mod_ns(j, Ns, magic);
       if (Ns > 1) {
         if constexpr (R == 4) {
-          const float2 w1 = __ldg(tw + k), w2 = cmul(w1, w1);
+          const float2 w1 = tw4(tw, k, Ns), w2 = cmul(w1, w1);
           v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
         } else {
 #pragma unroll
@@ -445,7 +452,7 @@ struct CtPlan {
   }
   static constexpr int ns(int p) { return p == 0 ? 1 : ns(p - 1) * radix(p - 1); }
   static constexpr int twoff(int p) {
-    return p == 0 ? 0 : twoff(p - 1) + ns(p - 1) * (radix(p - 1) == 4 ? 1 : radix(p - 1) - 1);
+    return p == 0 ? 0 : twoff(p - 1) + (int)tw_entries((uint32_t)radix(p - 1), (uint32_t)ns(p - 1));
   }
   static_assert(M == (1 << a) * ct_pow3(b) && M <= 16384, "M must be 2^a 3^b <= 16384");
 };
@@ -502,7 +509,7 @@ SPX_DEV void ct_pass(float2* s, const float2* __restrict__ tw, uint32_t tid) {
       const uint32_t k = j % Ns;
       const float2* t = tw + PL::twoff(P) + k;
       if constexpr (R == 4) {
-        const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
+        const float2 w1 = tw4(tw + PL::twoff(P), k, Ns), w2 = cmul(w1, w1);
         v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
       } else {
 #pragma unroll
@@ -552,7 +559,7 @@ SPX_DEV void ct_last_pass_out(const float2* s, const float2* __restrict__ tw, ui
     if (B % T == 0 || q + 1 < Q || j < (uint32_t)B) {
       const float2* t = tw + PL::twoff(P) + j;  // k = j mod Ns = j
       if constexpr (R == 4) {
-        const float2 w1 = __ldg(t), w2 = cmul(w1, w1);
+        const float2 w1 = tw4(tw + PL::twoff(P), j, Ns), w2 = cmul(w1, w1);
         v[q][1] = cmul(v[q][1], w1); v[q][2] = cmul(v[q][2], w2); v[q][3] = cmul(v[q][3], cmul(w2, w1));
       } else {
 #pragma unroll

@@ -208,7 +208,7 @@ bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept, uint32_t pref_local) {
     r.ns[p] = Ns;
     r.twoff[p] = off;
     r.nsmagic[p] = Ns > 1 ? (uint32_t)(((1ull << 32) + Ns - 1) / Ns) : 0u;
-    off += Ns * tw_rows(rad[p]);
+    off += tw_entries(rad[p], Ns);
     Ns *= rad[p];
   }
   uint32_t T = (r.M + ept - 1) / ept;
@@ -226,6 +226,20 @@ static inline float2 twiddle(uint64_t m, uint64_t L) {
   m %= L;
   const double a = -2.0 * M_PI * (double)m / (double)L;
   return make_float2((float)std::cos(a), (float)std::sin(a));
+}
+
+void fill_local_twiddles(const FftGeom& g, float2* twl) {
+  for (uint32_t p = 0; p < g.npass; ++p) {
+    const uint32_t R = g.radix[p], Ns = g.ns[p];
+    const uint64_t L = (uint64_t)Ns * R;
+    if (tw_split(R, Ns)) {
+      for (uint32_t l = 0; l < 64; ++l) twl[g.twoff[p] + l] = twiddle(l, L);
+      for (uint32_t j = 0; j < (Ns + 63) / 64; ++j) twl[g.twoff[p] + 64 + j] = twiddle(64ull * j, L);
+      continue;
+    }
+    for (uint32_t r = 1; r <= tw_rows(R); ++r)
+      for (uint32_t k = 0; k < Ns; ++k) twl[g.twoff[p] + (r - 1) * Ns + k] = twiddle((uint64_t)r * k, L);
+  }
 }
 
 FftPlan::~FftPlan() {
@@ -274,12 +288,7 @@ spx_status get_plan(spx_ctx* ctx, uint32_t nfft, const FftPlan** out) {
   }
   const FftGeom& g = plan->g;
   std::vector<float2> twl(std::max<uint32_t>(g.M, 1));
-  for (uint32_t p = 0; p < g.npass; ++p) {
-    const uint32_t R = g.radix[p], Ns = g.ns[p];
-    for (uint32_t r = 1; r <= tw_rows(R); ++r)
-      for (uint32_t k = 0; k < Ns; ++k)
-        twl[g.twoff[p] + (r - 1) * Ns + k] = twiddle((uint64_t)r * k, (uint64_t)Ns * R);
-  }
+  fill_local_twiddles(g, twl.data());
   cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(twiddles)");
   e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);

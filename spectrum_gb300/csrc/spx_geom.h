@@ -24,6 +24,17 @@ constexpr uint32_t kMaxFftSmem = (16384u + 1024u) * 8u + 32768u;
 // W^3k = W^2k W^k in the pass: the last pass of a 16384-point FFT reads a
 // 32 KB table instead of 96 KB, which keeps it in L1 beside the window.
 constexpr uint32_t tw_rows(uint32_t R) { return R == 4 ? 1u : R - 1u; }
+// A radix-4 pass with Ns >= kTwSplitNs stores W^k = W_{4 Ns}^k (k < Ns) as
+// two factors, lo[l] = W^l (l < 64) then hi[j] = W^{64 j} (j < ceil(Ns / 64)),
+// and forms W^k = hi[k >> 6] * lo[k & 63] (tw4 in fft_core.cuh): the last
+// pass of a 16384-point FFT reads 1 KB of table instead of 32 KB, so the
+// other passes' twiddles and the window stay in L1.
+constexpr uint32_t kTwSplitNs = 1024;
+constexpr bool tw_split(uint32_t R, uint32_t Ns) { return R == 4 && Ns >= kTwSplitNs; }
+// Table entries of a pass of radix R and stride Ns.
+constexpr uint32_t tw_entries(uint32_t R, uint32_t Ns) {
+  return tw_split(R, Ns) ? 64u + (Ns + 63u) / 64u : Ns * tw_rows(R);
+}
 
 struct FftGeom {
   uint32_t nfft;

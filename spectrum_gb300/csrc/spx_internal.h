@@ -42,6 +42,10 @@ struct FftPlan {
 bool build_geom(uint32_t nfft, FftGeom* g, uint32_t ept = kEPTDefault,
                 uint32_t pref_local = kPrefLocalCluster);
 bool is_smooth23(uint32_t n);
+// The local passes' twiddle table of geometry g (FP64-generated, FP32 stored):
+// per pass, tw_rows(R) rows of W_{Ns R}^{r k}, or the two factors of a split
+// radix-4 table (tw_split); g.twoff gives each pass's first entry.
+void fill_local_twiddles(const FftGeom& g, float2* twl);
 
 
 }  // namespace spx
