@@ -426,6 +426,19 @@ spx_status spx_mlp_refine(spx_ctx* ctx, spx_mlp* mlp, const void* d_fft, uint32_
                           uint32_t n_point, uint32_t nfft, float sample_rate, uint32_t K,
                           spx_max_value* d_peaks, const uint32_t* d_counts,
                           float* d_amplitude, uint32_t* d_used_mlp);
+/* spx_fft_peaks (params->mode SPX_PEAK_TOPK, K <= 32) followed by
+ * spx_mlp_refine on its peaks, with the same results bit for bit.  Where one
+ * CTA holds a beam's spectrum and the network's 20 KB of weights fit in the
+ * spectrum's shared memory (2^a 3^b nfft from about 2600 to 16384 points),
+ * and the call is small (beams x nfft <= 2^21), this is ONE launch:
+ * transform, top-K search and the network on each peak, the spectrum never
+ * written to device memory; otherwise the three steps run (faster once many
+ * CTAs queue: one launch holds each SM while it stages the weights).  No reference counterpart (the
+ * reference refines with the parabola, fft_kernel_sources_rocm.hpp:228-239). */
+spx_status spx_fft_peaks_mlp(spx_ctx* ctx, spx_mlp* mlp, const void* d_in, uint32_t beams,
+                             uint32_t n_point, uint32_t nfft, uint32_t window,
+                             const spx_peak_params* params, spx_max_value* d_out,
+                             uint32_t* d_counts, float* d_amplitude, uint32_t* d_used_mlp);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -119,6 +119,7 @@ PROTOTYPES: dict[str, tuple] = {
     "spx_mlp_train_step": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _f, _vp]),
     "spx_mlp_train": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f, _f, _u64, _vp]),
     "spx_mlp_refine": (_i, [_vp, _vp, _vp, _u32, _u32, _u32, _f, _u32, _vp, _vp, _vp, _vp]),
+    "spx_fft_peaks_mlp": (_i, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
 }
 
 

@@ -30,6 +30,7 @@
 #include <cuda/atomic>
 
 #include "fft_core.cuh"
+#include "mlp_device.cuh"
 #include "spx_internal.h"
 
 namespace spx {
@@ -48,6 +49,12 @@ struct FusedArgs {
   uint32_t* counts;
   uint32_t n_point, start, end, cap, mode, K, refine;
   float fs, factor;         // factor <= 0: no threshold
+  // learned refinement of the top-K peaks (C == 1, mode TOPK): the network's
+  // BF16 products and FP32 biases (null: none), amplitude and used flags out
+  const __nv_bfloat16* mlp_pb;
+  const float* mlp_p;
+  float* amp;
+  uint32_t* used;
 };
 
 SPX_DEV uint32_t bucket_of(float m) { return (__float_as_uint(m) & 0x7fffffffu) >> 19; }
@@ -121,7 +128,80 @@ SPX_DEV MaxValueDev fused_max(uint32_t bin, float2 z, float yl, float yc, float 
 // ---------------------------------------------------------------------------
 // C == 1: the whole spectrum is in this CTA's shared memory.
 // ---------------------------------------------------------------------------
-SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red, const FftGeom& g,
+// Bin k of the spectrum in shared memory.
+struct SmemBins {
+  const float2* s;
+  SPX_DEV float2 operator()(uint32_t k) const { return s[sw(k)]; }
+};
+
+// Shared-memory words the learned refinement needs after the search (it
+// reuses the spectrum's): the weights, a 64-float row per warp, then per
+// peak a record (8 words), its features and a flag, then the peak count.
+constexpr size_t mlp_fused_words(uint32_t warps, uint32_t K) {
+  return sizeof(MlpWeights) / 4 + (size_t)warps * kH + (size_t)K * (8 + kIn + 1) + 1;
+}
+
+// The learned refinement of the top-K list held by warp 0 (lane l: entry l,
+// cnt entries): records and features from the spectrum in shared memory,
+// then the weights staged over the spectrum and one warp per peak running
+// mlp_forward_warp, with the arithmetic of mlp_refine_kernel.  Every thread
+// of the CTA calls it.
+__device__ __noinline__ void refine_topk_fused(float2* s, uint64_t mine, const FftGeom& g, uint32_t beam,
+                                              const FusedArgs& a, float bw) {
+  const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
+  float* base = reinterpret_cast<float*>(s);
+  MlpWeights& w = *reinterpret_cast<MlpWeights*>(base);
+  float* rows = base + sizeof(MlpWeights) / 4;          // [nw][kH]
+  MaxValueDev* rec = reinterpret_cast<MaxValueDev*>(rows + (size_t)nw * kH);  // [K]
+  float* feat = reinterpret_cast<float*>(rec + a.K);     // [K][kIn]
+  uint32_t* good = reinterpret_cast<uint32_t*>(feat + (size_t)a.K * kIn);  // [K]
+  uint32_t& s_cnt = good[a.K];  // (dynamic shared memory: the kernel asks for the 227 KB limit)
+  MaxValueDev mv{};
+  float fe[kIn];
+  bool ok = false;
+  uint32_t cnt = 0;
+  if (warp == 0) {
+    cnt = __popc(__ballot_sync(0xffffffffu, lane < a.K && mine != 0));
+    if (lane < cnt) {
+      const uint32_t k = ~(uint32_t)mine;
+      mv = fused_max(k, s[sw(k)], mag_rn(s[sw(k - 1)]), __uint_as_float((uint32_t)(mine >> 32)),
+                     mag_rn(s[sw(k + 1)]), bw, a.refine);
+      ok = peak_features_at(SmemBins{s}, a.n_point, g.nfft, k, fe);
+    }
+  }
+  __syncthreads();  // the spectrum is read; its space takes the weights and the peaks
+  if (warp == 0) {
+    if (lane == 0) {
+      s_cnt = cnt;
+      a.counts[beam] = cnt;
+    }
+    if (lane < cnt) {
+      rec[lane] = mv;
+      for (int i = 0; i < kIn; ++i) feat[(size_t)lane * kIn + i] = fe[i];
+      good[lane] = ok ? 1u : 0u;
+    }
+  }
+  mlp_stage(w, a.mlp_pb, a.mlp_p, tid, T);
+  __syncthreads();
+  cnt = s_cnt;
+  for (uint32_t j = warp; j < cnt; j += nw) {
+    const bool gd = good[j] != 0;
+    float y0 = 0.f, y1 = 0.f;
+    if (gd) mlp_forward_warp(w, feat + (size_t)j * kIn, rows + (size_t)warp * kH, lane, &y0, &y1);
+    __syncwarp();
+    if (lane == 0) {
+      MaxValueDev r = rec[j];
+      float amp;
+      const bool use = mlp_apply(r, gd, y0, y1, a.fs, g.nfft, &amp);
+      const size_t idx = (size_t)beam * a.K + j;
+      a.out[idx] = r;
+      if (a.amp) a.amp[idx] = amp;
+      if (a.used) a.used[idx] = use ? 1u : 0u;
+    }
+  }
+}
+
+SPX_DEV void peaks_single_cta(float2* s, uint32_t* shist, uint32_t* s_red, const FftGeom& g,
                               uint32_t beam, const FusedArgs& a) {
   const uint32_t tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t nw = T >> 5;
@@ -158,6 +238,7 @@ SPX_DEV void peaks_single_cta(const float2* s, uint32_t* shist, uint32_t* s_red,
     uint64_t* lists = reinterpret_cast<uint64_t*>(shist);  // histogram no longer needed
     __syncthreads();
     mine = merge_warp_lists(lists, mine, nw, a.K, warp, lane);
+    if (a.mlp_pb) return refine_topk_fused(s, mine, g, beam, a, bw);
     if (warp != 0) return;
     const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, lane < a.K && mine != 0));
     if (lane == 0) a.counts[beam] = cnt;
@@ -655,6 +736,11 @@ static bool mx_geometry(uint32_t span, uint32_t* C2, uint32_t* chunk) {
   return true;
 }
 
+bool fused_mlp_supported(const FftGeom& g, uint32_t K) {
+  return g.C == 1 && fused_supported(g, SPX_PEAK_TOPK) && K >= 1 && K <= 32 &&
+         2 * (size_t)g.Mpad >= mlp_fused_words(g.T / 32, K);
+}
+
 bool fused_supported(const FftGeom& g, uint32_t mode) {
   if (mode != SPX_PEAK_ALL && mode != SPX_PEAK_TOPK) return false;
   if (g.C == 1) return (kHist % g.T) == 0 && fused_smem(g) <= 227 * 1024;
@@ -712,10 +798,16 @@ spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_i
                             uint32_t beams, uint32_t n_point, const float* d_win,
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
-                            uint32_t* d_counts) {
+                            uint32_t* d_counts, const MlpRefineArgs* mlp) {
   if (beams == 0) return SPX_OK;
   FftGeom g = plan.g;
   FusedArgs a{};
+  if (mlp) {
+    a.mlp_pb = static_cast<const __nv_bfloat16*>(mlp->pb);
+    a.mlp_p = mlp->p;
+    a.amp = mlp->amp;
+    a.used = mlp->used;
+  }
   a.in = d_in;
   a.win = d_win;
   a.tw_local = plan.d_tw_local;

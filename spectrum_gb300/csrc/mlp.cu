@@ -29,18 +29,12 @@
 #include <new>
 #include <vector>
 
+#include "mlp_device.cuh"
 #include "spx_device.cuh"
 #include "spx_internal.h"
 
 namespace spx {
 
-constexpr int kIn = 10, kH = 64, kOut = 2;
-constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kIn, kOffW2 = kOffB1 + kH,
-              kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH, kOffB3 = kOffW3 + kOut * kH,
-              kNParams = kOffB3 + kOut;  // 4994
-static_assert(kNParams == 4994, "parameter layout");
-
-SPX_DEV float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
 SPX_DEV float gelu_grad(float z) {
   return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) +
          z * 0.39894228040143268f * expf(-0.5f * z * z);
@@ -167,28 +161,14 @@ __global__ void mlp_gather_kernel(const float* __restrict__ feat, const float* _
 }
 
 // ---- features -------------------------------------------------------------------
-SPX_DEV float wrap_pi(float a) {
-  const float tp = 6.28318530717958647692f;
-  return a - tp * rintf(a * 0.15915494309189535f);
-}
-
-// Features of the peak at bin k (needs bins k-2..k+2); false at the edges or
-// when |X[k]| is 0.
+// Features of the peak at bin k of a spectrum in device memory (needs bins
+// k-2..k+2); false at the edges or when |X[k]| is 0.
+struct GlobalBins {
+  const float2* f;
+  SPX_DEV float2 operator()(uint32_t k) const { return f[k]; }
+};
 SPX_DEV bool peak_features(const float2* f, uint32_t n_point, uint32_t nfft, uint32_t k, float* feat) {
-  if (k < 2 || k + 2 >= nfft) return false;
-  const float2 c = f[k];
-  const float mc = mag_rn(c);
-  if (!(mc > 0.f)) return false;
-  const float lin = 3.14159265358979324f * (float)(n_point - 1) / (float)nfft;
-#pragma unroll
-  for (int d = -2; d <= 2; ++d) {
-    const float2 z = f[k + d];
-    feat[d + 2] = mag_rn(z) / mc;
-    // z * conj(c)
-    const float re = fmaf(z.x, c.x, z.y * c.y), im = fmaf(z.y, c.x, -z.x * c.y);
-    feat[d + 7] = d == 0 ? 0.f : wrap_pi(atan2f(im, re) + lin * (float)d);
-  }
-  return true;
+  return peak_features_at(GlobalBins{f}, n_point, nfft, k, feat);
 }
 
 // ---- training data ----------------------------------------------------------------
@@ -288,13 +268,14 @@ __global__ void frame_labels_kernel(const float2* __restrict__ X, const float2* 
   valid[fr] = ok ? 1u : 0u;
 }
 
-// ---- fused inference: one warp per peak ------------------------------------------
-// Lane l owns hidden units l and l + 32 of both layers; the layer-1 outputs go
-// through a per-warp shared row; the 2 outputs are warp sums.  Weights are
-// staged once per block in shared memory (BF16 values widened to FP32, exact).
+// ---- inference: one warp per peak ------------------------------------------------
+// mlp_forward_warp (mlp_device.cuh): lane l owns hidden units l and l + 32 of
+// both layers; the layer-1 outputs go through a per-warp shared row; the 2
+// outputs are warp sums.  Weights are staged once per block in shared memory
+// (BF16 values widened to FP32, exact).
 constexpr int kRefineWarps = 8;
 struct RefineSmem {
-  float w1[kH * kIn], b1[kH], w2[kH * kH], b2[kH], w3[kOut * kH], b3[kOut];
+  MlpWeights w;
   float h[kRefineWarps][kH];
   float x[kRefineWarps][kIn];
 };
@@ -307,14 +288,7 @@ mlp_refine_kernel(const __nv_bfloat16* __restrict__ pb, const float* __restrict_
                   uint32_t* __restrict__ used_mlp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RefineSmem& s = *reinterpret_cast<RefineSmem*>(smem_raw);
-  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) s.w1[i] = __bfloat162float(pb[kOffW1 + i]);
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) s.w2[i] = __bfloat162float(pb[kOffW2 + i]);
-  for (int i = threadIdx.x; i < kOut * kH; i += blockDim.x) s.w3[i] = __bfloat162float(pb[kOffW3 + i]);
-  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-    s.b1[i] = p[kOffB1 + i];
-    s.b2[i] = p[kOffB2 + i];
-  }
-  if (threadIdx.x < kOut) s.b3[threadIdx.x] = p[kOffB3 + threadIdx.x];
+  mlp_stage(s.w, pb, p, threadIdx.x, blockDim.x);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t total = (uint64_t)beams * K;
@@ -332,43 +306,13 @@ mlp_refine_kernel(const __nv_bfloat16* __restrict__ pb, const float* __restrict_
     good = __shfl_sync(0xffffffffu, good, 0);
     __syncwarp();
     float y0 = 0.f, y1 = 0.f;
-    if (good) {
-      float a0 = s.b1[lane], a1 = s.b1[lane + 32];
-#pragma unroll
-      for (int i = 0; i < kIn; ++i) {
-        const float xi = s.x[warp][i];
-        a0 = fmaf(xi, s.w1[lane * kIn + i], a0);
-        a1 = fmaf(xi, s.w1[(lane + 32) * kIn + i], a1);
-      }
-      s.h[warp][lane] = gelu(a0);
-      s.h[warp][lane + 32] = gelu(a1);
-      __syncwarp();
-      float c0 = s.b2[lane], c1 = s.b2[lane + 32];
-#pragma unroll 16
-      for (int i = 0; i < kH; ++i) {
-        const float hi = s.h[warp][i];
-        c0 = fmaf(hi, s.w2[lane * kH + i], c0);
-        c1 = fmaf(hi, s.w2[(lane + 32) * kH + i], c1);
-      }
-      const float g0 = gelu(c0), g1 = gelu(c1);
-      y0 = fmaf(g0, s.w3[lane], g1 * s.w3[lane + 32]);
-      y1 = fmaf(g0, s.w3[kH + lane], g1 * s.w3[kH + lane + 32]);
-      for (int o = 16; o > 0; o >>= 1) {
-        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
-        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
-      }
-      y0 += s.b3[0];
-      y1 += s.b3[1];
-    }
+    if (good) mlp_forward_warp(s.w, s.x[warp], s.h[warp], lane, &y0, &y1);
     __syncwarp();
     if (lane == 0) {
-      const bool use = good && isfinite(y0) && isfinite(y1) && fabsf(y0) <= 0.5f;
-      if (use) {
-        mv.freq_offset = y0;
-        mv.refined_frequency = __fmul_rn(__fadd_rn((float)mv.index, y0), __fdiv_rn(fs, (float)nfft));
-        peaks[idx] = mv;
-      }
-      if (amp_out) amp_out[idx] = use ? mv.magnitude * expf(y1) : mv.magnitude;
+      float amp;
+      const bool use = mlp_apply(mv, good, y0, y1, fs, nfft, &amp);
+      if (use) peaks[idx] = mv;
+      if (amp_out) amp_out[idx] = amp;
       if (used_mlp) used_mlp[idx] = use ? 1u : 0u;
     }
   }
@@ -392,6 +336,14 @@ struct spx_mlp {
   size_t work_floats = 0;
   uint64_t step = 0;              // Adam step count
 };
+
+namespace spx {
+void mlp_device_params(const spx_mlp* mlp, const void** pb, const float** p, int* device) {
+  *pb = mlp->d_pb;
+  *p = mlp->d_p;
+  *device = mlp->device;
+}
+}  // namespace spx
 
 namespace {
 

@@ -126,11 +126,24 @@ spx_status launch_fft_huge(spx_ctx* ctx, const FftPlan& plan, const float2* d_in
 
 // Fused FFT + peak search (fft_peaks.cu).
 bool fused_supported(const FftGeom& g, uint32_t mode);
+// The learned refinement inside the single-CTA top-K launch: the network's
+// BF16 products and FP32 biases, and the amplitude / used outputs (may be null).
+struct MlpRefineArgs {
+  const void* pb;
+  const float* p;
+  float* amp;
+  uint32_t* used;
+};
+// Whether geometry g's single-CTA kernel can refine K peaks per beam with the
+// network in its shared memory (C == 1 and room for the weights).
+bool fused_mlp_supported(const FftGeom& g, uint32_t K);
 spx_status launch_fft_peaks(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
                             uint32_t beams, uint32_t n_point, const float* d_win,
                             uint32_t mode, uint32_t start, uint32_t end, uint32_t cap_or_k,
                             float fs, uint32_t refine, float factor, spx_max_value* d_out,
-                            uint32_t* d_counts);
+                            uint32_t* d_counts, const MlpRefineArgs* mlp = nullptr);
+// The device weights of a network (mlp.cu).
+void mlp_device_params(const spx_mlp* mlp, const void** pb, const float** p, int* device);
 // Output of C spectrum rows per beam (rows[beam][k1][q] = X[k1 + C*q], the
 // exchange-slot layout) to bin order in any output mode (fft_kernels.cu).
 spx_status launch_rows_transpose(spx_ctx* ctx, const FftGeom& g, const float2* rows, uint32_t beams,

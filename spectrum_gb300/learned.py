@@ -27,6 +27,7 @@ import struct
 
 import numpy as np
 
+from . import _capi
 from ._capi import lib
 
 N_IN, N_HIDDEN, N_OUT = 10, 64, 2
@@ -212,6 +213,28 @@ class MLPRefiner:
                                           float(sample_rate), k, _ptr(peaks), _ptr(counts),
                                           _ptr(amp), _ptr(used)))
         return amp, used
+
+    def fft_peaks(self, x, nfft: int, window: int, k: int, sample_rate: float = 1.0,
+                  refine: int = 1, search_start: int = 0, search_end: int = 0, thresh_sigma: float = 0.0):
+        """The top-K search of spx_fft_peaks on samples x [beams, n_point]
+        complex64 with this network's refinement of every peak (one launch
+        where the beam's spectrum fits one CTA): returns (peaks [beams, K, 8]
+        int32 MaxValue words, counts [beams], amplitude [beams, K], used
+        [beams, K]), the bits of fft_peaks + refine."""
+        import torch
+        from . import PEAK_TOPK, _require_cuda
+        _require_cuda(x, torch.complex64, "x")
+        x2 = x.reshape(-1, x.shape[-1])
+        beams, n_point = x2.shape
+        out = torch.zeros((beams, k, 8), dtype=torch.int32, device=x.device)
+        counts = torch.zeros(beams, dtype=torch.int32, device=x.device)
+        amp = torch.zeros((beams, k), dtype=torch.float32, device=x.device)
+        used = torch.zeros((beams, k), dtype=torch.int32, device=x.device)
+        p = _capi.peak_params(PEAK_TOPK, search_start, search_end, 0, k, refine, sample_rate, thresh_sigma)
+        self.ctx.bind_stream()
+        self.ctx.check(lib.spx_fft_peaks_mlp(self.ctx.h, self.h, _ptr(x2), beams, n_point, int(nfft), int(window),
+                                             C.byref(p), _ptr(out), _ptr(counts), _ptr(amp), _ptr(used)))
+        return out, counts, amp, used
 
 
 def _check_rows(t, width, name):

@@ -213,6 +213,40 @@ def test_learned_beats_parabolic_inference_workload(spx, trained, cuda):
             assert abs(amp[b, 0].item() - par["magnitude"][b] * np.exp(y[0, 1])) < 1e-4 * par["magnitude"][b]
 
 
+@pytest.mark.parametrize("beams,n,k,sigma,win", [
+    (256, 8192, 1, 0.0, 1),    # the inference workload's shape, 2^21 points (one launch)
+    (512, 8192, 1, 0.0, 1),    # 2^22 points: spectrum, search, refinement
+    (16, 4096, 8, 0.0, 1),     # one launch, K = 8
+    (8, 16384, 3, 3.0, 4),     # one launch, threshold, Blackman-Harris
+    (12, 6561, 4, 0.0, 2),     # 3-smooth, one launch
+    (8, 1024, 2, 0.0, 1),      # too small for the weights: spectrum, search, refinement
+])
+def test_fft_peaks_mlp_matches_the_three_steps(spx, trained, cuda, beams, n, k, sigma, win):
+    """spx_fft_peaks_mlp (transform, top-K and the network on every peak in one
+    launch where the spectrum and the weights fit one CTA) gives the records,
+    amplitudes and used flags of spx_fft + spx_topk + spx_mlp_refine, bit for
+    bit."""
+    from spectrum_gb300 import synth
+    r, _, _ = trained
+    bs = synth.make_beams([n] * beams, tones=(1, 3), snr_db=(10.0, 30.0), seed=n + k)
+    xd = synth.synth_torch(bs, device=cuda)
+    out, counts, amp, used = r.fft_peaks(xd, n, win, k, sample_rate=2.0, thresh_sigma=sigma)
+    spec = spx.fft(xd, n, window=win)
+    o2, c2 = spx.topk(spec, k, sample_rate=2.0, refine=spx.REFINE_PARABOLIC, thresh_sigma=sigma)
+    a2, u2 = r.refine(spec, o2, c2, n, 2.0)
+    np.testing.assert_array_equal(counts.cpu().numpy(), c2.cpu().numpy())
+    c = counts.cpu().numpy()
+    g1, g2 = spx.maxvalues_to_numpy(out), spx.maxvalues_to_numpy(o2)
+    a1, a2n, u1, u2n = amp.cpu().numpy(), a2.cpu().numpy(), used.cpu().numpy(), u2.cpu().numpy()
+    for b in range(beams):
+        m = int(c[b])
+        for f in ("index", "real", "imag", "magnitude", "phase", "freq_offset", "refined_frequency"):
+            np.testing.assert_array_equal(g1[b, :m][f], g2[b, :m][f], err_msg=f"beam {b} {f}")
+        np.testing.assert_array_equal(a1[b, :m], a2n[b, :m])
+        np.testing.assert_array_equal(u1[b, :m], u2n[b, :m])
+    assert u1.sum() > 0  # the network was used somewhere
+
+
 def test_save_load_round_trip(learned, trained, cuda, tmp_path):
     import torch
     r, _, _ = trained
