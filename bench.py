@@ -584,7 +584,7 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
     bs = synth.workload_uneven(seed=2)
     xu = synth.synth_torch(bs, device=dev, packed=True)
     b = Batch(bs.lengths, window=spx.WINDOW_HANN, k=8, sample_rate=1.0, ctx=ctx)
-    b.autotune(xu)
+    _, tune_changed = b.autotune(xu)
     ms_one = _time_ms(stream, lambda: b.run(xu), 20)
     ms_same_kernels = _time_ms(stream, lambda: b.run_per_size(xu), 10)
     side = torch.cuda.Stream(device=dev)   # graph capture needs a non-default stream
@@ -635,7 +635,10 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
         rows_s.append(spx.fft(beam, nffts_u[i], window=spx.WINDOW_HANN).cpu().numpy()[0])
     res["uneven"] = {"config": "1024 beams, n_point U[1000,100000], nFFT = next 2^a3^b, Hann, top-8",
                      "samples": samples, "distinct_nfft": len(first),
-                     "ms_one_launch": round(ms_one, 4), "ms_graph_replay": round(ms_graph, 4),
+                     "ms_batch_run": round(ms_one, 4), "ms_graph_replay": round(ms_graph, 4),
+                     "batch_run": "spx_batch_run: one launch of every beam's FFT (clusters), then one "
+                                  "top-K launch; the autotuner's local sizes and cluster size",
+                     "batch_plans": {"cluster": int(b.cluster), "changed_by_autotune": int(tune_changed)},
                      "ms_plain_per_beam_eager": round(ms_plain, 4),
                      "ms_plain_per_beam_graph": round(ms_plain_graph, 4),
                      "plain_path": "1024 spx_fft_peaks calls, one per beam (TOPK 8, Hann)",
