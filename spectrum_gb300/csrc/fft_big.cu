@@ -2,16 +2,19 @@
 // workload's 2^20-point beams; 2^21 = the reference's nextPow2(2^20) x
 // repeat_count 2), beyond what one cluster holds on chip.
 //
-// nfft = Cb * M with M = 16384 and Cb in {32, 64, 128}; n = M*n1 + n2, k = k1 + Cb*k2:
+// nfft = Cb * M, n = M*n1 + n2, k = k1 + Cb*k2:
 //   launch 1 (big_cols_kernel): for each n2, the Cb-point DFT over n1 of the
 //     windowed, zero-padded samples, times W_N^{n2 k1}, written to
 //     scratch[beam][k1][n2] (device memory);
-//   launch 2 (big_rows_kernel): for each (beam, k1), the M-point Stockham FFT
-//     of row k1 (the passes of fft_core.cuh), X[k1 + Cb*k2] written back over
-//     the row it read (scratch[beam][k1][k2], one coalesced pass);
-//   launch 3 (rows_transpose_kernel, fft_kernels.cu): scratch[beam][k1][k2]
-//     -> bin k1 + Cb*k2 of the output in the requested mode, written in
-//     contiguous runs (written straight from launch 2, the stride-Cb stores
+//   2^19 and 2^20 (M = 4096, Cb = 128 or 256): launch 2 (big_rows4_kernel)
+//     transforms four rows k1 = 4r .. 4r+3 per CTA and writes bins
+//     4r .. 4r+3 + Cb*k2 of the output in the requested mode: runs of four
+//     bins, one 32-byte sector, so no separate reordering pass;
+//   2^21 (M = 16384, Cb = 128): launch 2 (big_rows_kernel) transforms row k1
+//     and writes X[k1 + Cb*k2] back over the row it read; launch 3
+//     (rows_transpose_kernel, fft_kernels.cu) writes bin order in the
+//     requested mode in contiguous runs (a 16384-point row per CTA leaves no
+//     room for four rows, and stride-Cb stores straight from the row kernel
 //     kept its SMs waiting on the store queue: 0.63 ms for 64 x 2^20 points).
 // All twiddles are FP64-generated and stored in FP32 (W_N^{n2 k1} in a table
 // of nfft entries laid out [k1][n2], so a warp's 32 columns read 256
@@ -26,16 +29,25 @@
 
 namespace spx {
 
-constexpr uint32_t kBigM = 16384;
+constexpr uint32_t kBigM = 16384;     // row length of the 2^21-point transform
+constexpr uint32_t kBigM4 = 4096;     // row length of the 2^19 / 2^20-point transforms
+constexpr uint32_t kRows4 = 4;        // rows per CTA of big_rows4_kernel
 
-// One tile = 32 consecutive n2 columns x Cb rows (n1); lane = column, warp
-// t = row group (tile reads conflict-free, output rows written 256 bytes at a time).
-template <int CB>
-__global__ void __launch_bounds__(256)
+// Row length M of a big transform of nfft points.
+static uint32_t big_rows(uint32_t nfft) { return nfft <= (1u << 20) ? kBigM4 : kBigM; }
+
+// One tile = 32 consecutive n2 columns x Cb rows (n1) in shared memory; lane
+// = column, warp t < G = row group (tile reads conflict-free, output rows
+// written 256 bytes at a time); rows of M points.  Cb = G x J: stage 1 is the
+// J-point DFT over rows t + G j, stage 2 the G-point DFT over t.
+template <int CB, int G>
+__global__ void __launch_bounds__(32 * G)
 big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
                 const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch,
-                uint32_t ahead) {
-  __shared__ float2 tile[CB][33];
+                uint32_t ahead, uint32_t M) {
+  extern __shared__ float2 tile_raw[];
+  float2(*tile)[33] = reinterpret_cast<float2(*)[33]>(tile_raw);  // [CB][33]
+  constexpr uint32_t NT = 32 * G;
   const uint32_t tid = threadIdx.x;
   const uint32_t beam = blockIdx.y, n2_0 = blockIdx.x * 32;
   const float2* x = in + (size_t)beam * n_point;
@@ -43,21 +55,21 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
     const uint64_t f = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x + ahead;
     if (ahead && f < (uint64_t)gridDim.x * gridDim.y && tid < CB) {
       const uint32_t fb = (uint32_t)(f / gridDim.x), fc = (uint32_t)(f % gridDim.x) * 32;
-      const uint32_t lo = tid * kBigM + fc, hi = min(lo + 32, n_point);
+      const uint32_t lo = tid * M + fc, hi = min(lo + 32, n_point);
       if (lo < hi) prefetch_l2(in + (size_t)fb * n_point + lo, (size_t)(hi - lo) * sizeof(float2), 0, 1);
     }
   }
-  for (uint32_t e = tid; e < CB * 32; e += 256) {
+  for (uint32_t e = tid; e < CB * 32; e += NT) {
     const uint32_t n1 = e >> 5, col = e & 31;
-    tile[n1][col] = load_sample(x, n1 * kBigM + n2_0 + col, n_point, win);
+    tile[n1][col] = load_sample(x, n1 * M + n2_0 + col, n_point, win);
   }
   __syncthreads();
   const uint32_t col = tid & 31, t = tid >> 5;
-  constexpr int J = CB / 8;  // stage-1 radix (4, 8 or 16)
-  // stage 1: thread t transforms rows t + 8j (j < J), twiddles W_CB^{t a}
+  constexpr int J = CB / G;  // stage-1 radix
+  // stage 1: thread t transforms rows t + G j (j < J), twiddles W_CB^{t a}
   float2 v[J];
 #pragma unroll
-  for (int j = 0; j < J; ++j) v[j] = tile[t + 8 * j][col];
+  for (int j = 0; j < J; ++j) v[j] = tile[t + G * j][col];
   Dft<J>::run(v);
 #pragma unroll
   for (int a = 1; a < J; ++a) {
@@ -66,21 +78,21 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
   }
   __syncthreads();
 #pragma unroll
-  for (int a = 0; a < J; ++a) tile[t + 8 * a][col] = v[a];
+  for (int a = 0; a < J; ++a) tile[t + G * a][col] = v[a];
   __syncthreads();
-  // stage 2: for a = t, t + 8, ... (< J), the 8-point DFT over t' of rows t' + 8a -> k1 = a + J*b
+  // stage 2: for a = t, t + G, ... (< J), the G-point DFT over t' of rows t' + G a -> k1 = a + J b
 #pragma unroll
-  for (uint32_t a = t; a < (uint32_t)J; a += 8) {
-    float2 w[8];
+  for (uint32_t a = t; a < (uint32_t)J; a += G) {
+    float2 w[G];
 #pragma unroll
-    for (int tp = 0; tp < 8; ++tp) w[tp] = tile[tp + 8 * a][col];
-    Dft<8>::run(w);
+    for (int tp = 0; tp < G; ++tp) w[tp] = tile[tp + G * a][col];
+    Dft<G>::run(w);
     const uint32_t n2 = n2_0 + col;
     float2* o = scratch + (size_t)beam * nfft + n2;
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
+    for (int b = 0; b < G; ++b) {
       const uint32_t k1 = a + J * b;
-      o[(size_t)k1 * kBigM] = cmul(w[b], __ldg(twN + (size_t)k1 * kBigM + n2));  // W_N^{n2 k1}
+      o[(size_t)k1 * M] = cmul(w[b], __ldg(twN + (size_t)k1 * M + n2));  // W_N^{n2 k1}
     }
   }
 }
@@ -105,21 +117,47 @@ big_rows_kernel(FftGeom g, const float2* __restrict__ tw_local, float2* __restri
   for (uint32_t i = tid; i < g.M; i += T) __stcs(row + i, s[sw(i)]);
 }
 
+// Four rows k1 = r0 .. r0+3 of 4096 points per CTA (four groups of 256
+// threads, one row each, in shared memory rows kRowPad4 elements apart), then
+// the bins r0 + q + Cb*k2 (q < 4) in the requested mode: each run of four
+// bins is one 32-byte sector of the output.  The row pitch puts the four rows
+// of one k2 on different bank pairs for a half-warp's reads.
+constexpr uint32_t kRowPad4 = sw_len(kBigM4) + 4;
+
+__global__ void __launch_bounds__(kRows4 * 256, 1)
+big_rows4_kernel(FftGeom g, const float2* __restrict__ tw_local, const float2* __restrict__ scratch,
+                 void* __restrict__ out, uint32_t out_mode, float scale) {
+  extern __shared__ float2 s[];
+  constexpr uint32_t TG = 256;
+  const uint32_t tid = threadIdx.x, grp = tid / TG;
+  const uint32_t per_beam = g.C / kRows4;
+  const uint32_t beam = blockIdx.x / per_beam, r0 = (blockIdx.x - beam * per_beam) * kRows4;
+  const float2* row = scratch + (size_t)beam * g.nfft + (size_t)(r0 + grp) * kBigM4;
+  // every group runs the same passes, so the plan's CTA barriers hold for all four
+  ct_local_fft<(int)kBigM4, (int)TG>(s + (size_t)grp * kRowPad4, SampleLoader{row, kBigM4, nullptr}, tw_local,
+                                     tid - grp * TG);
+  for (uint32_t e = tid; e < kRows4 * kBigM4; e += kRows4 * TG) {
+    const uint32_t k2 = e / kRows4, q = e - k2 * kRows4;
+    store_bin(out, out_mode, scale, g, beam, r0 + q + g.C * k2, s[(size_t)q * kRowPad4 + sw(k2)]);
+  }
+}
+
 bool big_size(uint32_t nfft) { return nfft == (1u << 19) || nfft == (1u << 20) || nfft == (1u << 21); }
 
-// Geometry of the row FFTs (M = 16384, C = Cb as the output stride) and the
+// Geometry of the row FFTs (M points, C = Cb as the output stride) and the
 // W_N table; called by get_plan for big sizes.
 spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
+  const uint32_t M = big_rows(nfft);
   FftGeom gl{};
-  if (!build_geom(kBigM, &gl, kEPTDefault)) return fail(ctx, SPX_ERR_INVALID_ARG, "big plan");
+  if (!build_geom(M, &gl, kEPTDefault)) return fail(ctx, SPX_ERR_INVALID_ARG, "big plan");
   gl.nfft = nfft;
-  gl.C = nfft / kBigM;
+  gl.C = nfft / M;
   plan->g = gl;
   plan->big = true;
-  std::vector<float2> twl(kBigM);
+  std::vector<float2> twl(M);
   fill_local_twiddles(gl, twl.data());
-  // [k1][n2] = W_N^{n2 k1} (n2 < kBigM, k1 < Cb, so n2 k1 < nfft: no reduction),
-  // then the Cb entries W_Cb^e = W_N^{e kBigM}
+  // [k1][n2] = W_N^{n2 k1} (n2 < M, k1 < Cb, so n2 k1 < nfft: no reduction),
+  // then the Cb entries W_Cb^e = W_N^{e M}
   const uint32_t cb = gl.C;
   std::vector<float2> twn((size_t)nfft + cb);
   auto w_n = [nfft](uint64_t m) {
@@ -127,8 +165,8 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
     return make_float2((float)std::cos(a), (float)std::sin(a));
   };
   for (uint32_t k1 = 0; k1 < cb; ++k1)
-    for (uint32_t n2 = 0; n2 < kBigM; ++n2) twn[(size_t)k1 * kBigM + n2] = w_n((uint64_t)n2 * k1);
-  for (uint32_t e = 0; e < cb; ++e) twn[(size_t)nfft + e] = w_n((uint64_t)e * kBigM);
+    for (uint32_t n2 = 0; n2 < M; ++n2) twn[(size_t)k1 * M + n2] = w_n((uint64_t)n2 * k1);
+  for (uint32_t e = 0; e < cb; ++e) twn[(size_t)nfft + e] = w_n((uint64_t)e * M);
   cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
   if (e == cudaSuccess) e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&plan->d_tw_cross, twn.size() * sizeof(float2));
@@ -146,21 +184,33 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   spx_status st = get_scratch(ctx, kSlotExchange, (size_t)beams * g.nfft * sizeof(float2), &scr);
   if (st != SPX_OK) return st;
   float2* scratch = static_cast<float2*>(scr);
-  dim3 grid(kBigM / 32, beams);
-  const void* kcols = g.C == 128 ? (const void*)big_cols_kernel<128>
-                      : g.C == 64 ? (const void*)big_cols_kernel<64> : (const void*)big_cols_kernel<32>;
-  const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, 256, 0, 1);
-  if (g.C == 128)
-    big_cols_kernel<128><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
-                                                        ahead_cols);
-  else if (g.C == 64)
-    big_cols_kernel<64><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
-                                                       ahead_cols);
-  else
-    big_cols_kernel<32><<<grid, 256, 0, ctx->stream>>>(d_in, n_point, d_win, plan.d_tw_cross, g.nfft, scratch,
-                                                       ahead_cols);
-  cudaError_t e = cudaGetLastError();
+  const uint32_t M = g.M;
+  const dim3 grid(M / 32, beams);
+  // Cb = 128 (2^19 as 128 x 4096, 2^21 as 128 x 16384: 8 x 16) or 256 (2^20
+  // as 256 x 4096: 16 x 16, 512 threads, two 16-point stages)
+  const void* kcols = g.C == 256 ? (const void*)big_cols_kernel<256, 16> : (const void*)big_cols_kernel<128, 8>;
+  const uint32_t cthreads = g.C == 256 ? 512u : 256u;
+  const size_t csmem = (size_t)g.C * 33 * sizeof(float2);
+  cudaError_t e = configure_kernel(kcols, csmem);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_cols_kernel");
+  const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, cthreads, csmem, 1);
+  void* cargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&plan.d_tw_cross, (void*)&g.nfft,
+                   (void*)&scratch, (void*)&ahead_cols, (void*)&M};
+  e = cudaLaunchKernel(kcols, grid, dim3(cthreads), cargs, csmem, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
+  if (M == kBigM4) {  // four rows per CTA, bin order written directly
+    const void* kfn = (const void*)big_rows4_kernel;
+    const size_t smem = (size_t)kRows4 * kRowPad4 * sizeof(float2);
+    e = configure_kernel(kfn, smem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows4_kernel");
+    FftGeom gg = g;
+    gg.beams = beams;
+    const float2* twl = plan.d_tw_local;
+    const float2* scr_c = scratch;
+    void* args[] = {(void*)&gg, (void*)&twl, (void*)&scr_c, (void*)&d_out, (void*)&out_mode, (void*)&scale};
+    e = cudaLaunchKernel(kfn, dim3(beams * (g.C / kRows4)), dim3(kRows4 * 256), args, smem, ctx->stream);
+    return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch big_rows4_kernel");
+  }
   const void* kfn = (const void*)big_rows_kernel<kEPTDefault>;
   e = configure_kernel(kfn, kMaxFftSmem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows_kernel");
