@@ -55,7 +55,8 @@ def test_fft_complex_matches_pocketfft(spx, cuda, nfft, n_point, win):
     assert e64 < FFT_TOL, f"vs FP64 pocketfft: {e64:.3e}"
 
 
-@pytest.mark.parametrize("nfft,n_point", [(4096, 4000), (131072, 65536), (13122, 13122)])
+@pytest.mark.parametrize("nfft,n_point", [(4096, 4000), (131072, 65536), (13122, 13122), (1 << 19, 400000),
+                                          (1 << 20, 1 << 20), (1 << 21, 1500000)])
 def test_fft_epilogues_consistent(spx, cuda, nfft, n_point):
     """MAG / MAG2 / MAGPHASE come from the same transform as COMPLEX."""
     import torch
@@ -253,7 +254,8 @@ def test_ifft_round_trip_and_fp64(spx, cuda, nfft):
 
 
 @pytest.mark.parametrize("n_point,nfft,win,full", [(1000, 1024, 1, False), (6000, 6561, 4, True),
-                                                   (30000, 32768, 2, False), (2187, 2187, 0, True)])
+                                                   (30000, 32768, 2, False), (2187, 2187, 0, True),
+                                                   (1000000, 1 << 20, 1, True), (300000, 1 << 19, 4, False)])
 def test_r2c_window_and_padding(spx, cuda, n_point, nfft, win, full):
     import torch
     if not spx.fft_size_supported(nfft):
