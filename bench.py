@@ -708,10 +708,26 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
     ms_ref = _time_ms(stream, lambda: (plain(), refine_only()), 10)
     a1 = torch.zeros((4096, 1), dtype=torch.float32, device=dev)
     u1 = torch.zeros((4096, 1), dtype=torch.int32, device=dev)
-    ms_one = _time_ms(stream, lambda: ctx.check(spx.lib.spx_fft_peaks_mlp(
-        ctx.h, r.h, C.c_void_p(xl.data_ptr()), 4096, nl, nl, spx.WINDOW_HANN, C.byref(p1),
-        C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr()), C.c_void_p(a1.data_ptr()),
-        C.c_void_p(u1.data_ptr()))), 10)
+    def peaks_mlp(beams):
+        return lambda: ctx.check(spx.lib.spx_fft_peaks_mlp(
+            ctx.h, r.h, C.c_void_p(xl.data_ptr()), beams, nl, nl, spx.WINDOW_HANN, C.byref(p1),
+            C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr()), C.c_void_p(a1.data_ptr()),
+            C.c_void_p(u1.data_ptr())))
+
+    def three_steps(beams):
+        def run():
+            ctx.check(spx.lib.spx_fft(ctx.h, C.c_void_p(xl.data_ptr()), beams, nl, nl, spx.WINDOW_HANN,
+                                      spx.OUT_COMPLEX, 1.0, C.c_void_p(specl.data_ptr())))
+            ctx.check(spx.lib.spx_topk(ctx.h, None, C.c_void_p(specl.data_ptr()), beams, nl, C.byref(p1),
+                                       C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr())))
+            ctx.check(spx.lib.spx_mlp_refine(ctx.h, r.h, C.c_void_p(specl.data_ptr()), beams, nl, nl, 1.0, 1,
+                                             C.c_void_p(o1.data_ptr()), C.c_void_p(c1.data_ptr()), None, None))
+        return run
+
+    ms_one = _time_ms(stream, peaks_mlp(4096), 10)
+    # 128 x 8192 = 2^20 points: spx_fft_peaks_mlp runs its single fused launch
+    ms_one_small = _time_ms(stream, peaks_mlp(128), 10)
+    ms_three_small = _time_ms(stream, three_steps(128), 10)
     ms_kernel = _time_ms(stream, refine_only, 10)
     plain()
     par = spx.maxvalues_to_numpy(o1)[:, 0].copy()
@@ -726,13 +742,17 @@ def bench_workloads(spx, ctx, stream, dev, hbm):
                       "make_frames_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
                       "final_loss": float(losses[-1]),
                       "ms_plain_fft_topk": round(ms_plain, 4), "ms_spx_fft_peaks_topk": round(ms_fused, 4),
-                      "ms_fft_topk_refine_one_launch": round(ms_one, 4),
+                      "ms_spx_fft_peaks_mlp": round(ms_one, 4),
+                      "spx_fft_peaks_mlp_path": "2^25 points per call: spx_fft, spx_topk and spx_mlp_refine "
+                                                "(one fused launch only up to 2^21 points per call)",
+                      "small_128x8192": {"ms_spx_fft_peaks_mlp_one_launch": round(ms_one_small, 4),
+                                         "ms_three_steps": round(ms_three_small, 4)},
                       "spx_fft_peaks_path": "spectrum to device memory + topk_kernel (the single-CTA fused "
                                             "kernel is taken up to 2^23 points per call)",
                       "ms_with_learned_refine": round(ms_ref, 4),
                       "ms_refine_kernel": round(ms_kernel, 4),
                       "Msamples_per_s_with_refine": round(4096 * nl / (ms_ref * 1e-3) / 1e6, 1),
-                      "Msamples_per_s_one_launch": round(4096 * nl / (ms_one * 1e-3) / 1e6, 1),
+                      "Msamples_per_s_spx_fft_peaks_mlp": round(4096 * nl / (ms_one * 1e-3) / 1e6, 1),
                       "freq_rms_bins_parabolic": round(rms_p, 6), "freq_rms_bins_learned": round(rms_m, 6),
                       "rms_gain": round(rms_p / rms_m, 2),
                       "fp64": fp64_error([xl[i].cpu().numpy() for i in range(0, 4096, 256)],

@@ -36,18 +36,19 @@ constexpr uint32_t kRows4 = 4;        // rows per CTA of big_rows4_kernel
 // Row length M of a big transform of nfft points.
 static uint32_t big_rows(uint32_t nfft) { return nfft <= (1u << 20) ? kBigM4 : kBigM; }
 
-// One tile = 32 consecutive n2 columns x Cb rows (n1) in shared memory; lane
-// = column, warp t < G = row group (tile reads conflict-free, output rows
-// written 256 bytes at a time); rows of M points.  Cb = G x J: stage 1 is the
-// J-point DFT over rows t + G j, stage 2 the G-point DFT over t.
+// One CTA = 32 consecutive n2 columns x Cb rows (n1); lane = column, warp
+// t < G = row group (every warp access is 32 consecutive columns of one row:
+// 256-byte global runs, conflict-free shared rows); rows of M points.
+// Cb = G x J: stage 1 is the J-point DFT over rows t + G j, on samples loaded
+// straight into registers (J loads in flight per thread); the shared tile
+// [Cb][32] only carries stage 1's outputs to stage 2, the G-point DFT over t.
 template <int CB, int G>
 __global__ void __launch_bounds__(32 * G)
 big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
                 const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch,
                 uint32_t ahead, uint32_t M) {
   extern __shared__ float2 tile_raw[];
-  float2(*tile)[33] = reinterpret_cast<float2(*)[33]>(tile_raw);  // [CB][33]
-  constexpr uint32_t NT = 32 * G;
+  float2(*tile)[32] = reinterpret_cast<float2(*)[32]>(tile_raw);  // [CB][32]
   const uint32_t tid = threadIdx.x;
   const uint32_t beam = blockIdx.y, n2_0 = blockIdx.x * 32;
   const float2* x = in + (size_t)beam * n_point;
@@ -59,24 +60,18 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
       if (lo < hi) prefetch_l2(in + (size_t)fb * n_point + lo, (size_t)(hi - lo) * sizeof(float2), 0, 1);
     }
   }
-  for (uint32_t e = tid; e < CB * 32; e += NT) {
-    const uint32_t n1 = e >> 5, col = e & 31;
-    tile[n1][col] = load_sample(x, n1 * M + n2_0 + col, n_point, win);
-  }
-  __syncthreads();
   const uint32_t col = tid & 31, t = tid >> 5;
   constexpr int J = CB / G;  // stage-1 radix
   // stage 1: thread t transforms rows t + G j (j < J), twiddles W_CB^{t a}
   float2 v[J];
 #pragma unroll
-  for (int j = 0; j < J; ++j) v[j] = tile[t + G * j][col];
+  for (int j = 0; j < J; ++j) v[j] = load_sample(x, (t + G * j) * M + n2_0 + col, n_point, win);
   Dft<J>::run(v);
 #pragma unroll
   for (int a = 1; a < J; ++a) {
     const uint32_t e = (t * a) % CB;
     v[a] = cmul(v[a], __ldg(twN + nfft + e));  // W_CB^e, after the [k1][n2] table
   }
-  __syncthreads();
 #pragma unroll
   for (int a = 0; a < J; ++a) tile[t + G * a][col] = v[a];
   __syncthreads();
@@ -190,7 +185,7 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   // as 256 x 4096: 16 x 16, 512 threads, two 16-point stages)
   const void* kcols = g.C == 256 ? (const void*)big_cols_kernel<256, 16> : (const void*)big_cols_kernel<128, 8>;
   const uint32_t cthreads = g.C == 256 ? 512u : 256u;
-  const size_t csmem = (size_t)g.C * 33 * sizeof(float2);
+  const size_t csmem = (size_t)g.C * 32 * sizeof(float2);
   cudaError_t e = configure_kernel(kcols, csmem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_cols_kernel");
   const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, cthreads, csmem, 1);
