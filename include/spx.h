@@ -167,8 +167,8 @@ uint32_t spx_next_pow2(uint32_t n);
 /* Smallest 2^a*3^b >= n (extension for beams of uneven length). */
 uint32_t spx_next_smooth23(uint32_t n);
 /* 1 if this build can transform nfft points; else 0.  2^a*3^b in
- * [2, 262144]: one pass (cluster of <= 16 CTAs); 2^19 .. 2^21: three
- * launches; 2^a*3^b above 2^21 up to 2^28 that split into two factors
+ * [2, 262144]: one pass (cluster of <= 16 CTAs); 2^19 and 2^20: two
+ * launches, 2^21: three; 2^a*3^b above 2^21 up to 2^28 that split into two factors
  * <= 16384 (every power of two): four steps with transposes; any other
  * length up to 2^27: Bluestein's chirp-z transform.  The reference takes any
  * nextPow2(n_point) * repeat_count (fft_processor_rocm.cpp:673-677). */
