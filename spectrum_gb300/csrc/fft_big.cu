@@ -128,6 +128,11 @@ big_rows4_kernel(FftGeom g, const float2* __restrict__ tw_local, const float2* _
   const uint32_t per_beam = g.C / kRows4;
   const uint32_t beam = blockIdx.x / per_beam, r0 = (blockIdx.x - beam * per_beam) * kRows4;
   const float2* row = scratch + (size_t)beam * g.nfft + (size_t)(r0 + grp) * kBigM4;
+  // the four rows of the CTA one residency wave later follow this CTA's
+  // (CTA b holds elements [b, b + 1) x kRows4 x kBigM4 of the scratch)
+  if (g.ahead && blockIdx.x + g.ahead < gridDim.x)
+    prefetch_l2(scratch + (size_t)(blockIdx.x + g.ahead) * (kRows4 * kBigM4), kRows4 * kBigM4 * sizeof(float2), tid,
+                kRows4 * TG);
   // every group runs the same passes, so the plan's CTA barriers hold for all four
   ct_local_fft<(int)kBigM4, (int)TG>(s + (size_t)grp * kRowPad4, SampleLoader{row, kBigM4, nullptr}, tw_local,
                                      tid - grp * TG);
@@ -200,6 +205,7 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
     if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_rows4_kernel");
     FftGeom gg = g;
     gg.beams = beams;
+    gg.ahead = ctx->input_on_host ? 0u : resident_ctas(kfn, kRows4 * 256, smem, 1);
     const float2* twl = plan.d_tw_local;
     const float2* scr_c = scratch;
     void* args[] = {(void*)&gg, (void*)&twl, (void*)&scr_c, (void*)&d_out, (void*)&out_mode, (void*)&scale};
