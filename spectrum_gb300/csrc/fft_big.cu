@@ -3,9 +3,9 @@
 // repeat_count 2), beyond what one cluster holds on chip.
 //
 // nfft = Cb * M, n = M*n1 + n2, k = k1 + Cb*k2:
-//   launch 1 (big_cols_kernel): for each n2, the Cb-point DFT over n1 of the
-//     windowed, zero-padded samples, times W_N^{n2 k1}, written to
-//     scratch[beam][k1][n2] (device memory);
+//   launch 1 (big_cols_kernel; big_cols_pipe_kernel for 2^19): for each n2,
+//     the Cb-point DFT over n1 of the windowed, zero-padded samples, times
+//     W_N^{n2 k1}, written to scratch[beam][k1][n2] (device memory);
 //   2^19 and 2^20 (M = 4096, Cb = 128 or 256): launch 2 (big_rows4_kernel)
 //     transforms four rows k1 = 4r .. 4r+3 per CTA and writes bins
 //     4r .. 4r+3 + Cb*k2 of the output in the requested mode: runs of four
@@ -21,6 +21,7 @@
 // contiguous bytes; W_M from the local plan), which is what the 120 dB
 // dynamic range of the precision workload needs.  Replaces hipFFT's internal
 // multi-pass plan for large sizes (src/fft_func/src/fft_processor_rocm.cpp:176-193).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -88,6 +89,93 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
     for (int b = 0; b < G; ++b) {
       const uint32_t k1 = a + J * b;
       o[(size_t)k1 * M] = cmul(w[b], __ldg(twN + (size_t)k1 * M + n2));  // W_N^{n2 k1}
+    }
+  }
+}
+
+// 8-byte asynchronous copy global -> shared (zero-filled when src_bytes is 0).
+SPX_DEV void cp_async8(void* dst, const void* src, uint32_t src_bytes) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+SPX_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+SPX_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// The column DFTs of big_cols_kernel in a persistent loop over the tiles
+// f = blockIdx.x, blockIdx.x + gridDim.x, ... (beam f / tpb, columns
+// 32 (f mod tpb) ..): while a CTA transforms tile f, the samples of its next
+// tile stream into shared memory by asynchronous copies.  Each thread copies
+// exactly the elements it reads itself (rows t + G j of its column), so the
+// landing buffer needs no barrier; stage 1's outputs alternate between two
+// exchange tiles, so one CTA barrier per tile orders every access.  The
+// arithmetic is big_cols_kernel's: the same bits.
+template <int CB, int G>
+__global__ void __launch_bounds__(32 * G, 2)
+big_cols_pipe_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __restrict__ win,
+                     const float2* __restrict__ twN, uint32_t nfft, float2* __restrict__ scratch, uint32_t M,
+                     uint32_t tpb, uint32_t total) {
+  extern __shared__ float2 tile_raw[];
+  float2(*land)[32] = reinterpret_cast<float2(*)[32]>(tile_raw);                 // [CB][32]
+  float2(*xch0)[32] = reinterpret_cast<float2(*)[32]>(tile_raw + CB * 32);       // [CB][32]
+  float2(*xch1)[32] = reinterpret_cast<float2(*)[32]>(tile_raw + 2 * CB * 32);   // [CB][32]
+  constexpr int J = CB / G;  // stage-1 radix
+  const uint32_t tid = threadIdx.x, col = tid & 31, t = tid >> 5;
+  auto issue = [&](uint32_t f) {  // this thread's samples of tile f into its landing slots
+    const uint32_t beam = f / tpb, n2_0 = (f - beam * tpb) * 32;
+    const float2* x = in + (size_t)beam * n_point;
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const uint32_t n = (t + G * j) * M + n2_0 + col;
+      const bool ok = n < n_point;
+      cp_async8(&land[t + G * j][col], ok ? x + n : x, ok ? 8u : 0u);
+    }
+    cp_async_commit();
+  };
+  uint32_t f = blockIdx.x;
+  if (f < total) issue(f);
+  for (uint32_t it = 0; f < total; ++it, f += gridDim.x) {
+    const uint32_t beam = f / tpb, n2_0 = (f - beam * tpb) * 32;
+    cp_async_wait_all();  // this thread's copies of tile f have landed
+    float2 v[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) v[j] = land[t + G * j][col];
+    if (win) {  // window of the samples inside the beam (load_sample's arithmetic)
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const uint32_t n = (t + G * j) * M + n2_0 + col;
+        if (n < n_point) {
+          const float w = __ldg(win + n);
+          v[j].x = __fmul_rn(v[j].x, w);
+          v[j].y = __fmul_rn(v[j].y, w);
+        }
+      }
+    }
+    Dft<J>::run(v);
+#pragma unroll
+    for (int a = 1; a < J; ++a) {
+      const uint32_t e = (t * a) % CB;
+      v[a] = cmul(v[a], __ldg(twN + nfft + e));  // W_CB^e
+    }
+    float2(*xch)[32] = (it & 1u) ? xch1 : xch0;
+#pragma unroll
+    for (int a = 0; a < J; ++a) xch[t + G * a][col] = v[a];
+    // the stores above depend on every landed value, so this thread's reads
+    // of its landing slots are complete before the slots are refilled
+    if (f + gridDim.x < total) issue(f + gridDim.x);
+    __syncthreads();
+    const uint32_t n2 = n2_0 + col;
+    float2* o = scratch + (size_t)beam * nfft + n2;
+#pragma unroll
+    for (uint32_t a = t; a < (uint32_t)J; a += G) {
+      float2 w[G];
+#pragma unroll
+      for (int tp = 0; tp < G; ++tp) w[tp] = xch[tp + G * a][col];
+      Dft<G>::run(w);
+#pragma unroll
+      for (int b = 0; b < G; ++b) {
+        const uint32_t k1 = a + J * b;
+        o[(size_t)k1 * M] = cmul(w[b], __ldg(twN + (size_t)k1 * M + n2));  // W_N^{n2 k1}
+      }
     }
   }
 }
@@ -185,19 +273,41 @@ spx_status launch_fft_big(spx_ctx* ctx, const FftPlan& plan, const float2* d_in,
   if (st != SPX_OK) return st;
   float2* scratch = static_cast<float2*>(scr);
   const uint32_t M = g.M;
-  const dim3 grid(M / 32, beams);
   // Cb = 128 (2^19 as 128 x 4096, 2^21 as 128 x 16384: 8 x 16) or 256 (2^20
   // as 256 x 4096: 16 x 16, 512 threads, two 16-point stages)
-  const void* kcols = g.C == 256 ? (const void*)big_cols_kernel<256, 16> : (const void*)big_cols_kernel<128, 8>;
   const uint32_t cthreads = g.C == 256 ? 512u : 256u;
-  const size_t csmem = (size_t)g.C * 32 * sizeof(float2);
-  cudaError_t e = configure_kernel(kcols, csmem);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_cols_kernel");
-  const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, cthreads, csmem, 1);
-  void* cargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&plan.d_tw_cross, (void*)&g.nfft,
-                   (void*)&scratch, (void*)&ahead_cols, (void*)&M};
-  e = cudaLaunchKernel(kcols, grid, dim3(cthreads), cargs, csmem, ctx->stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
+  cudaError_t e = cudaSuccess;
+  if (g.C == 128 && M == kBigM4 && !ctx->input_on_host) {
+    // 2^19, samples in device memory: the pipelined column kernel (96 KiB,
+    // two 256-thread CTAs per SM).
+    // Measured against big_cols_kernel (back-to-back calls, same bits):
+    // 128 x 2^19 0.505 -> 0.480 ms; for 2^20 (192 KiB, one 512-thread CTA per
+    // SM) 0.591 -> 0.615 ms and for 2^21 0.692 -> 0.696 ms, so those keep
+    // big_cols_kernel.
+    const void* kfn = (const void*)big_cols_pipe_kernel<128, 8>;
+    const size_t smem = 3 * (size_t)g.C * 32 * sizeof(float2);  // landing tile + two exchange tiles
+    e = configure_kernel(kfn, smem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_cols_pipe_kernel");
+    const uint32_t tpb = M / 32, total = tpb * beams;
+    const uint32_t resident = resident_ctas(kfn, cthreads, smem, 1);
+    if (resident == 0) return fail(ctx, SPX_ERR_CUDA, "big_cols_pipe_kernel: no resident CTA");
+    const uint32_t ctas = std::min(total, resident);
+    void* args[] = {(void*)&d_in,    (void*)&n_point, (void*)&d_win, (void*)&plan.d_tw_cross, (void*)&g.nfft,
+                    (void*)&scratch, (void*)&M,       (void*)&tpb,   (void*)&total};
+    e = cudaLaunchKernel(kfn, dim3(ctas), dim3(cthreads), args, smem, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_pipe_kernel");
+  } else {
+    const void* kcols =
+        g.C == 256 ? (const void*)big_cols_kernel<256, 16> : (const void*)big_cols_kernel<128, 8>;
+    const size_t csmem = (size_t)g.C * 32 * sizeof(float2);
+    e = configure_kernel(kcols, csmem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "configure big_cols_kernel");
+    const uint32_t ahead_cols = ctx->input_on_host ? 0u : resident_ctas(kcols, cthreads, csmem, 1);
+    void* cargs[] = {(void*)&d_in, (void*)&n_point, (void*)&d_win, (void*)&plan.d_tw_cross, (void*)&g.nfft,
+                     (void*)&scratch, (void*)&ahead_cols, (void*)&M};
+    e = cudaLaunchKernel(kcols, dim3(M / 32, beams), dim3(cthreads), cargs, csmem, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch big_cols_kernel");
+  }
   if (M == kBigM4) {  // four rows per CTA, bin order written directly
     const void* kfn = (const void*)big_rows4_kernel;
     const size_t smem = (size_t)kRows4 * kRowPad4 * sizeof(float2);
