@@ -55,6 +55,25 @@ def test_fft_complex_matches_pocketfft(spx, cuda, nfft, n_point, win):
     assert e64 < FFT_TOL, f"vs FP64 pocketfft: {e64:.3e}"
 
 
+def test_pipelined_column_tiles_match_single_tiles_and_pocketfft(spx, cuda):
+    """2^19 points run the pipelined column kernel: with 8 beams (1024 column
+    tiles) every CTA loops over several tiles, streaming the next one into
+    shared memory while it transforms the current one and alternating its two
+    exchange tiles.  Each beam equals the same beam transformed alone (128
+    tiles: one per CTA) bit for bit, and pocketfft within the tolerance."""
+    import torch
+    nfft, n_point = 1 << 19, 400000
+    x = _signal(8, n_point, 77)
+    xd = torch.from_numpy(x).to(cuda)
+    got = spx.fft(xd, nfft, window=spx.WINDOW_HANN).cpu().numpy()
+    for b in (0, 3, 7):
+        alone = spx.fft(xd[b:b + 1].contiguous(), nfft, window=spx.WINDOW_HANN).cpu().numpy()
+        assert np.array_equal(got[b:b + 1].view(np.uint32), alone.view(np.uint32)), f"beam {b}"
+    for b in (0, 7):
+        e32 = _max_rel(got[b:b + 1], orc.fft_fp32(x[b:b + 1], nfft, orc.WINDOW_HANN))
+        assert e32 < FFT_TOL, f"beam {b} vs FP32 pocketfft: {e32:.3e}"
+
+
 @pytest.mark.parametrize("nfft,n_point", [(4096, 4000), (131072, 65536), (13122, 13122), (1 << 19, 400000),
                                           (1 << 20, 1 << 20), (1 << 21, 1500000)])
 def test_fft_epilogues_consistent(spx, cuda, nfft, n_point):
