@@ -297,13 +297,20 @@ mlp_refine_kernel(const __nv_bfloat16* __restrict__ pb, const float* __restrict_
     const uint32_t beam = (uint32_t)(idx / K), j = (uint32_t)(idx % K);
     if (j >= counts[beam]) continue;  // warp-uniform
     MaxValueDev mv = peaks[idx];
-    bool good = false;
-    if (lane == 0) {
-      float fe[kIn];
-      good = peak_features(fft + (size_t)beam * nfft, n_point, nfft, mv.index, fe);
-      for (int i = 0; i < kIn; ++i) s.x[warp][i] = fe[i];
+    // the features, offset d = lane - 2 on lanes 0..4 (peak_features_at's
+    // arithmetic, one offset per lane)
+    const uint32_t k = mv.index;
+    const GlobalBins bins{fft + (size_t)beam * nfft};
+    bool good = k >= 2 && k + 2 < nfft;
+    float2 c = make_float2(0.f, 0.f);
+    float mc = 0.f;
+    if (good) {
+      c = bins(k);
+      mc = mag_rn(c);
+      good = mc > 0.f;
     }
-    good = __shfl_sync(0xffffffffu, good, 0);
+    if (good && lane < 5)
+      peak_feature_pair(bins, c, mc, peak_lin(n_point, nfft), k, (int)lane - 2, &s.x[warp][lane], &s.x[warp][lane + 5]);
     __syncwarp();
     float y0 = 0.f, y1 = 0.f;
     if (good) mlp_forward_warp(s.w, s.x[warp], s.h[warp], lane, &y0, &y1);

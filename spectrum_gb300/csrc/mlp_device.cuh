@@ -30,6 +30,25 @@ SPX_DEV float wrap_pi(float a) {
   return a - tp * rintf(a * 0.15915494309189535f);
 }
 
+// pi (n_point - 1) / nfft: the window centre's linear phase per bin.
+SPX_DEV float peak_lin(uint32_t n_point, uint32_t nfft) {
+  return 3.14159265358979324f * (float)(n_point - 1) / (float)nfft;
+}
+
+// The two features of offset d (-2..2) of the peak at bin k, whose bin is c
+// with |c| = mc > 0: |X[k+d]| / |X[k]| and the wrapped phase of
+// X[k+d] conj X[k] plus lin d (0 for d = 0).  Every path computes its
+// features through this function, so they have the same bits.
+template <typename Bin>
+SPX_DEV void peak_feature_pair(const Bin& bin, float2 c, float mc, float lin, uint32_t k, int d, float* ratio,
+                               float* phase) {
+  const float2 z = bin(k + d);
+  *ratio = mag_rn(z) / mc;
+  // z * conj(c)
+  const float re = fmaf(z.x, c.x, z.y * c.y), im = fmaf(z.y, c.x, -z.x * c.y);
+  *phase = d == 0 ? 0.f : wrap_pi(atan2f(im, re) + lin * (float)d);
+}
+
 // Features of the peak at bin k (bins k-2..k+2 through bin(k), complex);
 // false at the edges or when |X[k]| is 0.
 template <typename Bin>
@@ -38,28 +57,32 @@ SPX_DEV bool peak_features_at(const Bin& bin, uint32_t n_point, uint32_t nfft, u
   const float2 c = bin(k);
   const float mc = mag_rn(c);
   if (!(mc > 0.f)) return false;
-  const float lin = 3.14159265358979324f * (float)(n_point - 1) / (float)nfft;
+  const float lin = peak_lin(n_point, nfft);
 #pragma unroll
-  for (int d = -2; d <= 2; ++d) {
-    const float2 z = bin(k + d);
-    feat[d + 2] = mag_rn(z) / mc;
-    // z * conj(c)
-    const float re = fmaf(z.x, c.x, z.y * c.y), im = fmaf(z.y, c.x, -z.x * c.y);
-    feat[d + 7] = d == 0 ? 0.f : wrap_pi(atan2f(im, re) + lin * (float)d);
-  }
+  for (int d = -2; d <= 2; ++d) peak_feature_pair(bin, c, mc, lin, k, d, &feat[d + 2], &feat[d + 7]);
   return true;
 }
 
-// The weights in shared memory as FP32, in the parameter layout.
+// The weights in shared memory as FP32; the hidden layers' matrices
+// transposed to [input][unit] (w1t[i * kH + o] = W1[o][i], likewise w2t), so
+// the 32 lanes of a warp, one unit each, read 32 consecutive words: no bank
+// conflicts (the parameter layout [unit][input] put every lane of a warp on
+// one bank).  The layout does not change any sum's order.
 struct MlpWeights {
-  float w1[kH * kIn], b1[kH], w2[kH * kH], b2[kH], w3[kOut * kH], b3[kOut];
+  float w1t[kIn * kH], b1[kH], w2t[kH * kH], b2[kH], w3[kOut * kH], b3[kOut];
 };
 
 // Stages the weights (BF16 products, FP32 biases) by threads tid, tid + n, ...
 SPX_DEV void mlp_stage(MlpWeights& w, const __nv_bfloat16* __restrict__ pb, const float* __restrict__ p,
                        uint32_t tid, uint32_t n) {
-  for (uint32_t i = tid; i < kH * kIn; i += n) w.w1[i] = __bfloat162float(pb[kOffW1 + i]);
-  for (uint32_t i = tid; i < kH * kH; i += n) w.w2[i] = __bfloat162float(pb[kOffW2 + i]);
+  for (uint32_t i = tid; i < kH * kIn; i += n) {  // W1[o][c], i = o kIn + c
+    const uint32_t o = i / kIn, c = i - o * kIn;
+    w.w1t[c * kH + o] = __bfloat162float(pb[kOffW1 + i]);
+  }
+  for (uint32_t i = tid; i < kH * kH; i += n) {  // W2[o][c], i = o kH + c
+    const uint32_t o = i / kH, c = i - o * kH;
+    w.w2t[c * kH + o] = __bfloat162float(pb[kOffW2 + i]);
+  }
   for (uint32_t i = tid; i < kOut * kH; i += n) w.w3[i] = __bfloat162float(pb[kOffW3 + i]);
   for (uint32_t i = tid; i < kH; i += n) {
     w.b1[i] = p[kOffB1 + i];
@@ -77,8 +100,8 @@ SPX_DEV void mlp_forward_warp(const MlpWeights& w, const float* x, float* h, uin
 #pragma unroll
   for (int i = 0; i < kIn; ++i) {
     const float xi = x[i];
-    a0 = fmaf(xi, w.w1[lane * kIn + i], a0);
-    a1 = fmaf(xi, w.w1[(lane + 32) * kIn + i], a1);
+    a0 = fmaf(xi, w.w1t[i * kH + lane], a0);
+    a1 = fmaf(xi, w.w1t[i * kH + lane + 32], a1);
   }
   h[lane] = gelu(a0);
   h[lane + 32] = gelu(a1);
@@ -87,8 +110,8 @@ SPX_DEV void mlp_forward_warp(const MlpWeights& w, const float* x, float* h, uin
 #pragma unroll 16
   for (int i = 0; i < kH; ++i) {
     const float hi = h[i];
-    c0 = fmaf(hi, w.w2[lane * kH + i], c0);
-    c1 = fmaf(hi, w.w2[(lane + 32) * kH + i], c1);
+    c0 = fmaf(hi, w.w2t[i * kH + lane], c0);
+    c1 = fmaf(hi, w.w2t[i * kH + lane + 32], c1);
   }
   const float g0 = gelu(c0), g1 = gelu(c1);
   float s0 = fmaf(g0, w.w3[lane], g1 * w.w3[lane + 32]);
