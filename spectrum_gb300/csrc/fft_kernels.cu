@@ -125,10 +125,10 @@ fft_group_out_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
 // shared memory with a row pitch of tc + 1 (conflict-free both ways).
 __global__ void __launch_bounds__(256)
 rows_transpose_kernel(FftGeom g, const float2* __restrict__ rows, uint32_t tc, uint32_t cmagic,
-                      void* __restrict__ out, uint32_t out_mode, float scale) {
+                      void* __restrict__ out, uint32_t out_mode, float scale, uint32_t beam0) {
   extern __shared__ float2 tile[];  // [C][tc + 1]
   const uint32_t tid = threadIdx.x, C = g.C, M = g.M, ld = tc + 1;
-  const uint32_t beam = blockIdx.y, q0 = blockIdx.x * tc;
+  const uint32_t beam = beam0 + blockIdx.y, q0 = blockIdx.x * tc;
   const uint32_t tshift = 31u - __clz(tc);  // tc is a power of two
   const float2* src = rows + (size_t)beam * g.nfft + q0;
   for (uint32_t f = tid; f < C * tc; f += 256) {
@@ -149,10 +149,14 @@ spx_status launch_rows_transpose(spx_ctx* ctx, const FftGeom& g, const float2* r
   while (g.C * tc < 1024) tc *= 2;
   const uint32_t cmagic = 0xFFFFFFFFu / g.C + 1u;  // e div C = umulhi(e, cmagic) for e * C < 2^32
   const size_t smem = (size_t)g.C * (tc + 1) * sizeof(float2);
-  const dim3 grid((g.M + tc - 1) / tc, beams);
-  rows_transpose_kernel<<<grid, 256, smem, ctx->stream>>>(g, rows, tc, cmagic, d_out, out_mode, scale);
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? SPX_OK : cuda_fail(ctx, e, "launch rows_transpose_kernel");
+  constexpr uint32_t kMaxGridY = 65535;  // beams per launch (gridDim.y)
+  for (uint32_t b0 = 0; b0 < beams; b0 += kMaxGridY) {
+    const dim3 grid((g.M + tc - 1) / tc, std::min(beams - b0, kMaxGridY));
+    rows_transpose_kernel<<<grid, 256, smem, ctx->stream>>>(g, rows, tc, cmagic, d_out, out_mode, scale, b0);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "launch rows_transpose_kernel");
+  }
+  return SPX_OK;
 }
 
 bool group_geometry(const FftGeom& g) {

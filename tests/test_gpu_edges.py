@@ -57,6 +57,23 @@ def test_maximum_single_pass_and_two_launch_sizes(spx, cuda):
     assert not spx.fft_size_supported(1 << 29)
 
 
+def test_more_beams_than_one_grid_dimension(spx, cuda):
+    """65540 beams of a 32768-point transform (rows written to bin order by a
+    transpose whose grid holds at most 65535 beams per launch): beams on both
+    sides of the 65535 boundary equal pocketfft.  About 26 GB on the device."""
+    import torch
+    beams, n_point, nfft = 65540, 8, 32768
+    x = _rand(beams, n_point, 3)
+    got = spx.fft(torch.from_numpy(x).to(cuda), nfft, window=spx.WINDOW_NONE, out="mag2")
+    torch.cuda.synchronize()
+    for b in (0, 65534, 65535, 65536, beams - 1):
+        ref = np.abs(orc.fft_fp32(x[b:b + 1], nfft)) ** 2
+        row = got[b].cpu().numpy()
+        assert np.abs(row - ref[0]).max() / ref.max() < 1e-5, b
+    del got
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("start,end", [(1, 2), (1, 3), (0, 0), (1023, 1023), (1000, 4096), (2, 1024)])
 def test_all_maxima_windows_at_the_ends(spx, cuda, start, end):
     """Empty / one-bin windows, end beyond nfft (clipped to nfft-1), windows
