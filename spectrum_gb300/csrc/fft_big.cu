@@ -16,10 +16,14 @@
 //     requested mode in contiguous runs (a 16384-point row per CTA leaves no
 //     room for four rows, and stride-Cb stores straight from the row kernel
 //     kept its SMs waiting on the store queue: 0.63 ms for 64 x 2^20 points).
-// All twiddles are FP64-generated and stored in FP32 (W_N^{n2 k1} in a table
-// of nfft entries laid out [k1][n2], so a warp's 32 columns read 256
-// contiguous bytes; W_M from the local plan), which is what the 120 dB
-// dynamic range of the precision workload needs.  Replaces hipFFT's internal
+// All twiddles are FP64-generated and stored in FP32, which is what the
+// 120 dB dynamic range of the precision workload needs: W_N^{n2 k1}, k1 =
+// a + 16 b, as the product of two factor tables [a][n2] = W_N^{n2 a} and
+// [b][n2] = W_N^{16 n2 b} (a warp's 32 columns read 256 contiguous bytes of
+// each; a CTA's slice of the second, 4 KB, is read by all its warps from L1,
+// where the full [k1][n2] table of nfft entries came from L2: 64 x 2^20
+// 0.591 -> 0.580 ms, 128 x 2^19 0.479 -> 0.460 ms, max error vs FP64
+// 2.3e-7 -> 2.2e-7 of the peak); W_M from the local plan.  Replaces hipFFT's internal
 // multi-pass plan for large sizes (src/fft_func/src/fft_processor_rocm.cpp:176-193).
 #include <algorithm>
 #include <cmath>
@@ -71,7 +75,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
 #pragma unroll
   for (int a = 1; a < J; ++a) {
     const uint32_t e = (t * a) % CB;
-    v[a] = cmul(v[a], __ldg(twN + nfft + e));  // W_CB^e, after the [k1][n2] table
+    v[a] = cmul(v[a], __ldg(twN + (size_t)(J + G) * M + e));  // W_CB^e, after the two factor tables
   }
 #pragma unroll
   for (int a = 0; a < J; ++a) tile[t + G * a][col] = v[a];
@@ -85,10 +89,11 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
     Dft<G>::run(w);
     const uint32_t n2 = n2_0 + col;
     float2* o = scratch + (size_t)beam * nfft + n2;
+    const float2 ta = __ldg(twN + (size_t)a * M + n2);  // W_N^{n2 a}
 #pragma unroll
     for (int b = 0; b < G; ++b) {
-      const uint32_t k1 = a + J * b;
-      o[(size_t)k1 * M] = cmul(w[b], __ldg(twN + (size_t)k1 * M + n2));  // W_N^{n2 k1}
+      const uint32_t k1 = a + J * b;  // W_N^{n2 k1} = W_N^{n2 a} W_N^{n2 J b}
+      o[(size_t)k1 * M] = cmul(w[b], cmul(ta, __ldg(twN + (size_t)(J + b) * M + n2)));
     }
   }
 }
@@ -154,7 +159,7 @@ big_cols_pipe_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
 #pragma unroll
     for (int a = 1; a < J; ++a) {
       const uint32_t e = (t * a) % CB;
-      v[a] = cmul(v[a], __ldg(twN + nfft + e));  // W_CB^e
+      v[a] = cmul(v[a], __ldg(twN + (size_t)(J + G) * M + e));  // W_CB^e
     }
     float2(*xch)[32] = (it & 1u) ? xch1 : xch0;
 #pragma unroll
@@ -171,10 +176,11 @@ big_cols_pipe_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
 #pragma unroll
       for (int tp = 0; tp < G; ++tp) w[tp] = xch[tp + G * a][col];
       Dft<G>::run(w);
+      const float2 ta = __ldg(twN + (size_t)a * M + n2);  // W_N^{n2 a}
 #pragma unroll
       for (int b = 0; b < G; ++b) {
-        const uint32_t k1 = a + J * b;
-        o[(size_t)k1 * M] = cmul(w[b], __ldg(twN + (size_t)k1 * M + n2));  // W_N^{n2 k1}
+        const uint32_t k1 = a + J * b;  // W_N^{n2 k1} = W_N^{n2 a} W_N^{n2 J b}
+        o[(size_t)k1 * M] = cmul(w[b], cmul(ta, __ldg(twN + (size_t)(J + b) * M + n2)));
       }
     }
   }
@@ -244,17 +250,21 @@ spx_status build_big_plan(spx_ctx* ctx, uint32_t nfft, FftPlan* plan) {
   plan->big = true;
   std::vector<float2> twl(M);
   fill_local_twiddles(gl, twl.data());
-  // [k1][n2] = W_N^{n2 k1} (n2 < M, k1 < Cb, so n2 k1 < nfft: no reduction),
-  // then the Cb entries W_Cb^e = W_N^{e M}
-  const uint32_t cb = gl.C;
-  std::vector<float2> twn((size_t)nfft + cb);
+  // W_N^{n2 k1} for k1 = a + 16 b as two factor tables, [a][n2] = W_N^{n2 a}
+  // (a < 16) and [16 + b][n2] = W_N^{16 n2 b} (b < Cb / 16), then the Cb
+  // entries W_Cb^e = W_N^{e M}
+  const uint32_t cb = gl.C, J = 16, G = cb / J;
+  std::vector<float2> twn((size_t)(J + G) * M + cb);
   auto w_n = [nfft](uint64_t m) {
+    m %= nfft;
     const double a = -2.0 * M_PI * (double)m / (double)nfft;
     return make_float2((float)std::cos(a), (float)std::sin(a));
   };
-  for (uint32_t k1 = 0; k1 < cb; ++k1)
-    for (uint32_t n2 = 0; n2 < M; ++n2) twn[(size_t)k1 * M + n2] = w_n((uint64_t)n2 * k1);
-  for (uint32_t e = 0; e < cb; ++e) twn[(size_t)nfft + e] = w_n((uint64_t)e * M);
+  for (uint32_t a = 0; a < J; ++a)
+    for (uint32_t n2 = 0; n2 < M; ++n2) twn[(size_t)a * M + n2] = w_n((uint64_t)n2 * a);
+  for (uint32_t b = 0; b < G; ++b)
+    for (uint32_t n2 = 0; n2 < M; ++n2) twn[(size_t)(J + b) * M + n2] = w_n((uint64_t)n2 * J * b);
+  for (uint32_t e = 0; e < cb; ++e) twn[(size_t)(J + G) * M + e] = w_n((uint64_t)e * M);
   cudaError_t e = cudaMalloc(&plan->d_tw_local, twl.size() * sizeof(float2));
   if (e == cudaSuccess) e = cudaMemcpy(plan->d_tw_local, twl.data(), twl.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&plan->d_tw_cross, twn.size() * sizeof(float2));
