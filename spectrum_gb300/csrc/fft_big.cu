@@ -67,6 +67,7 @@ big_cols_kernel(const float2* __restrict__ in, uint32_t n_point, const float* __
   }
   const uint32_t col = tid & 31, t = tid >> 5;
   constexpr int J = CB / G;  // stage-1 radix
+  static_assert(J == 16, "the W_N factor tables are built for k1 = a + 16 b");
   // stage 1: thread t transforms rows t + G j (j < J), twiddles W_CB^{t a}
   float2 v[J];
 #pragma unroll
@@ -124,6 +125,7 @@ big_cols_pipe_kernel(const float2* __restrict__ in, uint32_t n_point, const floa
   float2(*xch0)[32] = reinterpret_cast<float2(*)[32]>(tile_raw + CB * 32);       // [CB][32]
   float2(*xch1)[32] = reinterpret_cast<float2(*)[32]>(tile_raw + 2 * CB * 32);   // [CB][32]
   constexpr int J = CB / G;  // stage-1 radix
+  static_assert(J == 16, "the W_N factor tables are built for k1 = a + 16 b");
   const uint32_t tid = threadIdx.x, col = tid & 31, t = tid >> 5;
   auto issue = [&](uint32_t f) {  // this thread's samples of tile f into its landing slots
     const uint32_t beam = f / tpb, n2_0 = (f - beam * tpb) * 32;
